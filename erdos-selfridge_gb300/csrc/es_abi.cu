@@ -1,0 +1,963 @@
+// Host side of the C ABI (include/es_gb300.h): validates a plan descriptor, derives every
+// device table in C++ (sorted inner ring, carry-split keys and buckets, ring-1 residue table,
+// ring-2 delta table, word-mask phase tables), uploads them in one arena per plan, and drives
+// single-plan launches (the reference GpuSieve._launch surface) and persistent batch launches
+// with CUDA-graph replay.  No exception crosses the ABI: every entry point returns an int.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/es_gb300.h"
+#include "es_internal.h"
+
+typedef unsigned __int128 u128;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+    g_err = msg;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+    g_err = std::string(what) + ": " + cudaGetErrorString(e);
+    return ES_ERR_CUDA;
+}
+
+#define ES_CUDA(call, what)                                  \
+    do {                                                     \
+        cudaError_t _e = (call);                             \
+        if (_e != cudaSuccess) return cuda_fail(_e, what);   \
+    } while (0)
+
+u128 mk(uint64_t lo, uint64_t hi) { return ((u128)hi << 64) | lo; }
+uint32_t bitlen128(u128 x) {
+    uint32_t n = 0;
+    while (x) { ++n; x >>= 1; }
+    return n;
+}
+uint32_t mod_q(u128 x, uint32_t q) { return (uint32_t)(x % q); }
+
+struct DeviceFacts {
+    int dev = -1;
+    int sms = 0;
+    int smem_optin = 0;
+    bool prepared = false;
+};
+DeviceFacts g_dev;
+
+int device_facts() {
+    int dev = 0;
+    ES_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
+    if (g_dev.dev == dev && g_dev.prepared) return ES_OK;
+    int major = 0, minor = 0;
+    ES_CUDA(cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev), "attr");
+    ES_CUDA(cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev), "attr");
+    if (major != 10 || minor != 3)
+        return fail(ES_ERR_NODEV, "device is sm_" + std::to_string(major * 10 + minor) +
+                                      ", this library is built for sm_103a only");
+    g_dev.dev = dev;
+    ES_CUDA(cudaDeviceGetAttribute(&g_dev.sms, cudaDevAttrMultiProcessorCount, dev), "attr");
+    ES_CUDA(cudaDeviceGetAttribute(&g_dev.smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev),
+            "attr");
+    int e = es_scan_prepare(g_dev.smem_optin - 1024);
+    if (e) return cuda_fail((cudaError_t)e, "cudaFuncSetAttribute(scan)");
+    g_dev.prepared = true;
+    return ES_OK;
+}
+
+size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+int check_tune(const es_tune& t) {
+    if (t.layout != ES_LAYOUT_WORDMASK && t.layout != ES_LAYOUT_SCALAR)
+        return fail(ES_ERR_ARG, "tune.layout must be 0 (word-mask) or 1 (scalar)");
+    if (t.mask_filters < 1 || t.mask_filters > ES_MAX_MASK_FILTERS)
+        return fail(ES_ERR_ARG, "tune.mask_filters must be in 1..8");
+    if (t.threads < 64 || t.threads > 512 || t.threads % 32)
+        return fail(ES_ERR_ARG, "tune.threads must be a multiple of 32 in [64, 512]");
+    if (t.strip < 1 || t.strip > 4096) return fail(ES_ERR_ARG, "tune.strip must be in 1..4096");
+    if (t.ctas_per_sm < 1 || t.ctas_per_sm > 16)
+        return fail(ES_ERR_ARG, "tune.ctas_per_sm must be in 1..16");
+    return ES_OK;
+}
+
+es_tune default_tune() {
+    es_tune t;
+    t.layout = ES_LAYOUT_WORDMASK;
+    t.mask_filters = 4;
+    t.threads = 256;
+    t.strip = 4;
+    t.smem_kb = 200;
+    t.ctas_per_sm = 1;
+    t.count_stages = 1;
+    t.reserved = 0;
+    return t;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------------------------------
+struct es_ctx {
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    es_tune tune{};
+    EsInst h_inst{};
+    EsInst* d_inst = nullptr;
+    unsigned char* d_arena = nullptr;
+    size_t arena_bytes = 0;
+    uint64_t table_bytes = 0;
+    std::vector<uint32_t> q;
+    std::vector<uint32_t> fast_words_mask;  // prefix words of word-mask tables, F_built + 1
+    std::vector<uint32_t> fast_words_bits;  // prefix words of bit tables, n_filters + 1
+    u128 M = 1;
+    uint32_t tconst[ES_MAX_FILTERS] = {0};
+    uint64_t t = 0;
+    // launch state
+    unsigned long long* d_counts = nullptr;
+    es_survivor* d_surv = nullptr;
+    uint64_t surv_cap = 0;
+    unsigned long long* d_surv_n = nullptr;
+    unsigned long long* d_unit = nullptr;
+    unsigned long long* d_found = nullptr;
+    unsigned long long* d_min = nullptr;
+    unsigned long long* h_pin = nullptr;  // pinned scalars for small readbacks
+    uint64_t* d_list = nullptr;
+    uint64_t list_cap = 0;
+    bool launched = false;
+};
+
+struct es_batch {
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    es_tune tune{};
+    std::vector<es_ctx*> ctxs;
+    std::vector<EsItem> h_items;
+    std::vector<uint32_t> nf_of_item;
+    uint32_t n_groups = 0;
+    EsItem* d_items = nullptr;
+    uint32_t* d_tconst = nullptr;
+    unsigned long long* d_counts = nullptr;
+    uint64_t counts_words = 0;
+    std::vector<uint64_t> count_off;
+    es_survivor* d_surv = nullptr;
+    uint64_t surv_cap = 0;
+    unsigned long long* d_surv_n = nullptr;
+    unsigned long long* d_unit = nullptr;
+    unsigned long long* d_found = nullptr;
+    unsigned long long* d_min = nullptr;
+    EsLaunch L{};
+    int grid = 0;
+    bool ran = false;
+};
+
+namespace {
+
+// Shared-memory plan of one launch: [small | fast tables | tconst | counters].
+struct SmemPlan {
+    uint32_t fast_off, tconst_off, cnt_off, bytes;
+    uint32_t fast_words_cap;
+};
+
+SmemPlan plan_smem(uint32_t small_max, uint32_t nf_max, const es_tune& tune, uint32_t fast_need) {
+    SmemPlan p;
+    const uint32_t fixed_tail = (uint32_t)align_up(4u * nf_max, 16) * 2u;
+    uint32_t budget = tune.smem_kb * 1024u;
+    const uint32_t optin = (uint32_t)(g_dev.smem_optin - 1024);
+    if (budget > optin) budget = optin;
+    uint32_t avail = budget > small_max + fixed_tail ? budget - small_max - fixed_tail : 0u;
+    uint32_t fast_bytes = std::min<uint32_t>(avail, 4u * fast_need);
+    fast_bytes = (uint32_t)(fast_bytes / 16u * 16u);
+    p.fast_off = small_max;
+    p.fast_words_cap = fast_bytes / 4u;
+    p.tconst_off = p.fast_off + fast_bytes;
+    p.cnt_off = p.tconst_off + (uint32_t)align_up(4u * nf_max, 16);
+    p.bytes = p.cnt_off + (uint32_t)align_up(4u * nf_max, 16);
+    return p;
+}
+
+// Largest prefix of fast tables (by filter) that fits cap words, among the first F filters.
+void fast_prefix(const es_ctx* c, uint32_t layout, uint32_t F, uint32_t cap, uint32_t* n_sm,
+                 uint32_t* words) {
+    const std::vector<uint32_t>& pre = layout == ES_LAYOUT_WORDMASK ? c->fast_words_mask
+                                                                     : c->fast_words_bits;
+    uint32_t lim = std::min<uint32_t>(F, (uint32_t)pre.size() - 1);
+    uint32_t n = 0;
+    while (n < lim && pre[n + 1] <= cap) ++n;
+    *n_sm = n;
+    *words = pre[n];
+}
+
+uint32_t fast_need(const es_ctx* c, uint32_t layout, uint32_t F) {
+    const std::vector<uint32_t>& pre = layout == ES_LAYOUT_WORDMASK ? c->fast_words_mask
+                                                                     : c->fast_words_bits;
+    return pre[std::min<uint32_t>(F, (uint32_t)pre.size() - 1)];
+}
+
+int grid_for(uint32_t layout, uint32_t count, const es_tune& tune, uint32_t smem, uint64_t units,
+             int* grid) {
+    int occ = 0;
+    int e = es_scan_occupancy((int)layout, (int)count, tune.mask_filters, (int)tune.threads,
+                              (int)smem, &occ);
+    if (e) return cuda_fail((cudaError_t)e, "occupancy");
+    if (occ < 1) return fail(ES_ERR_ARG, "launch shape does not fit one SM (threads/smem)");
+    uint64_t g = (uint64_t)g_dev.sms * (uint64_t)std::min<uint32_t>((uint32_t)occ, tune.ctas_per_sm);
+    if (units < g) g = units;
+    if (g < 1) g = 1;
+    *grid = (int)g;
+    return ES_OK;
+}
+
+uint64_t cycles_of(const EsInst& I, uint64_t ob, uint64_t oe, uint64_t* cb) {
+    *cb = ob / I.r1;
+    const uint64_t ce = (oe + I.r1 - 1) / I.r1;
+    return ce - *cb;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------------------------------
+extern "C" {
+
+const char* es_last_error(void) { return g_err.c_str(); }
+
+int es_abi_version(void) { return ES_ABI_VERSION; }
+
+int es_device_info(int* sm_count, int* cc_major, int* cc_minor, uint64_t* smem_optin_bytes) {
+    int dev = 0;
+    ES_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
+    int a = 0, b = 0, s = 0, o = 0;
+    ES_CUDA(cudaDeviceGetAttribute(&a, cudaDevAttrComputeCapabilityMajor, dev), "attr");
+    ES_CUDA(cudaDeviceGetAttribute(&b, cudaDevAttrComputeCapabilityMinor, dev), "attr");
+    ES_CUDA(cudaDeviceGetAttribute(&s, cudaDevAttrMultiProcessorCount, dev), "attr");
+    ES_CUDA(cudaDeviceGetAttribute(&o, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev), "attr");
+    if (sm_count) *sm_count = s;
+    if (cc_major) *cc_major = a;
+    if (cc_minor) *cc_minor = b;
+    if (smem_optin_bytes) *smem_optin_bytes = (uint64_t)o;
+    return ES_OK;
+}
+
+int es_ctx_destroy(es_ctx* c) {
+    if (!c) return ES_OK;
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    cudaFree(c->d_arena);
+    cudaFree(c->d_counts);
+    cudaFree(c->d_surv);
+    cudaFree(c->d_surv_n);
+    cudaFree(c->d_list);
+    if (c->h_pin) cudaFreeHost(c->h_pin);
+    if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->ev1) cudaEventDestroy(c->ev1);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return ES_OK;
+}
+
+int es_ctx_create(const es_plan_desc* d, const es_tune* tune_in, es_ctx** out) {
+    if (!d || !out) return fail(ES_ERR_ARG, "null descriptor or output pointer");
+    *out = nullptr;
+    es_tune tune = tune_in ? *tune_in : default_tune();
+    if (int e = check_tune(tune)) return e;
+    if (d->flags != 0) return fail(ES_ERR_ARG, "descriptor flags must be 0");
+    const u128 M = mk(d->M_lo, d->M_hi);
+    if (M == 0 || bitlen128(M) > 126) return fail(ES_ERR_RANGE, "wheel modulus must be in [1, 2^126)");
+    if (d->n_filters > ES_MAX_FILTERS)
+        return fail(ES_ERR_RANGE, "too many residual filters (max " + std::to_string(ES_MAX_FILTERS) + ")");
+    if (d->n_rings > ES_MAX_RINGS - 3) return fail(ES_ERR_RANGE, "too many wheel rings");
+    if (d->n_rings && (!d->radix || !d->term_lo || !d->term_hi))
+        return fail(ES_ERR_ARG, "null ring arrays");
+    if (d->n_filters && (!d->filter_q || !d->allowed)) return fail(ES_ERR_ARG, "null filter arrays");
+    if (int e = device_facts()) return e;
+
+    // ---- rings (padded to >= 3 with radix-1 rings whose only term is 0) -------------------
+    std::vector<uint32_t> radix;
+    std::vector<u128> terms;
+    std::vector<uint32_t> roff;
+    uint64_t R = 1;
+    size_t pos = 0;
+    for (uint32_t j = 0; j < d->n_rings; ++j) {
+        const uint32_t r = d->radix[j];
+        if (r == 0 || r > 65535) return fail(ES_ERR_RANGE, "ring radix must be in [1, 65535]");
+        roff.push_back((uint32_t)terms.size());
+        radix.push_back(r);
+        for (uint32_t i = 0; i < r; ++i, ++pos) {
+            const u128 v = mk(d->term_lo[pos], d->term_hi[pos]);
+            if (v >= M) return fail(ES_ERR_ARG, "ring term not reduced mod M");
+            terms.push_back(v);
+        }
+        if (R > (1ull << 62) / r) return fail(ES_ERR_RANGE, "residues per block exceed 2^62");
+        R *= r;
+    }
+    while (radix.size() < 3) {
+        roff.push_back((uint32_t)terms.size());
+        radix.push_back(1);
+        terms.push_back(0);
+    }
+    const uint32_t nr = (uint32_t)radix.size();
+    const uint32_t r0 = radix[0], r1 = radix[1], r2 = radix[2];
+    const uint32_t nf = d->n_filters;
+    const uint32_t FB = std::min<uint32_t>(ES_FMAX, nf);
+    const uint32_t W = (r0 + 31) / 32;
+
+    es_ctx* c = new (std::nothrow) es_ctx();
+    if (!c) return fail(ES_ERR_NOMEM, "host allocation");
+    c->tune = tune;
+    c->M = M;
+    c->q.assign(d->filter_q, d->filter_q + nf);
+
+    // ---- filters ------------------------------------------------------------------------
+    std::vector<EsFilterC> fc(nf);
+    std::vector<uint32_t> bit_off(nf + 1, 0);
+    for (uint32_t f = 0; f < nf; ++f) {
+        const uint32_t q = c->q[f];
+        if (q < 2 || q >= ES_MAX_Q) {
+            es_ctx_destroy(c);
+            return fail(ES_ERR_RANGE, "filter modulus must be in [2, 2^20)");
+        }
+        bit_off[f + 1] = bit_off[f] + (q + 31) / 32;
+        fc[f].q = q;
+        fc[f].corr = (uint32_t)((q - mod_q(M, q)) % q);
+        fc[f].w1 = mod_q((u128)1 << 32, q);
+        fc[f].w2 = mod_q((u128)1 << 64, q);
+        fc[f].w3 = mod_q((u128)1 << 96, q);
+        fc[f].off = bit_off[f];
+        fc[f].rcp = (uint64_t)(((u128)1 << 64) / q);
+    }
+    c->fast_words_bits = bit_off;
+    auto admissible = [&](uint32_t f, uint32_t r) -> uint32_t {
+        return (d->allowed[bit_off[f] + (r >> 5)] >> (r & 31u)) & 1u;
+    };
+
+    // ---- inner ring: sorted slots, keys, buckets ----------------------------------------
+    std::vector<uint32_t> order(r0);
+    for (uint32_t i = 0; i < r0; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](uint32_t a, uint32_t b) { return terms[roff[0] + a] < terms[roff[0] + b]; });
+    std::vector<u128> S0(r0);
+    for (uint32_t i = 0; i < r0; ++i) S0[i] = terms[roff[0] + order[i]];
+    const uint32_t bl = bitlen128(M);
+    const uint32_t sh = bl > 32 ? bl - 32 : 0;
+    const uint32_t kbits = bitlen128(M >> sh);
+    const uint32_t bsh = kbits > 10 ? kbits - 10 : 0;
+    std::vector<uint32_t> K0(r0);
+    for (uint32_t i = 0; i < r0; ++i) K0[i] = (uint32_t)(S0[i] >> sh);
+    std::vector<uint16_t> BK(ES_NBUCKET + 1);
+    for (uint32_t bkt = 0; bkt <= ES_NBUCKET; ++bkt) {
+        const uint64_t lim = (uint64_t)bkt << bsh;
+        uint32_t n = 0;
+        while (n < r0 && (uint64_t)K0[n] < lim) ++n;
+        BK[bkt] = (uint16_t)n;
+    }
+
+    // ---- small block ----------------------------------------------------------------------
+    EsInst& I = c->h_inst;
+    size_t off = 0;
+    auto take = [&](size_t bytes) { size_t o = off; off = align_up(off + bytes, 16); return (uint32_t)o; };
+    I.o_T1 = take(16ull * r1);
+    I.o_TQ1 = take(4ull * ES_FMAX * r1);
+    I.o_D2 = take(16ull * r2);
+    I.o_DQ2 = take(4ull * ES_FMAX * r2);
+    I.o_S0 = take(16ull * r0);
+    I.o_K0 = take(4ull * r0);
+    I.o_I0 = take(4ull * r0);
+    I.o_Q0 = take(4ull * ES_FMAX * r0);
+    I.o_BK = take(2ull * (ES_NBUCKET + 1));
+    I.o_FC = take(sizeof(EsFilterC) * std::max<uint32_t>(nf, 1));
+    const size_t small_bytes = off;
+    std::vector<unsigned char> small(small_bytes, 0);
+    auto put128 = [&](uint32_t o, uint32_t i, u128 v) {
+        uint64_t lo = (uint64_t)v, hi = (uint64_t)(v >> 64);
+        memcpy(&small[o + 16ull * i], &lo, 8);
+        memcpy(&small[o + 16ull * i + 8], &hi, 8);
+    };
+    auto put32 = [&](uint32_t o, uint32_t i, uint32_t v) { memcpy(&small[o + 4ull * i], &v, 4); };
+    for (uint32_t i = 0; i < r1; ++i) {
+        const u128 v = terms[roff[1] + i];
+        put128(I.o_T1, i, v);
+        for (uint32_t f = 0; f < FB; ++f) put32(I.o_TQ1, i * ES_FMAX + f, mod_q(v, c->q[f]));
+    }
+    for (uint32_t i = 0; i < r2; ++i) {
+        const u128 a = terms[roff[2] + i], b = terms[roff[2] + (i + 1) % r2];
+        const u128 dlt = b >= a ? b - a : b + (M - a);
+        put128(I.o_D2, i, dlt);
+        for (uint32_t f = 0; f < FB; ++f) put32(I.o_DQ2, i * ES_FMAX + f, mod_q(dlt, c->q[f]));
+    }
+    for (uint32_t i = 0; i < r0; ++i) {
+        put128(I.o_S0, i, S0[i]);
+        put32(I.o_K0, i, K0[i]);
+        put32(I.o_I0, i, order[i]);
+        for (uint32_t f = 0; f < FB; ++f) put32(I.o_Q0, f * r0 + i, mod_q(S0[i], c->q[f]));
+    }
+    memcpy(&small[I.o_BK], BK.data(), 2ull * (ES_NBUCKET + 1));
+    if (nf) memcpy(&small[I.o_FC], fc.data(), sizeof(EsFilterC) * nf);
+
+    // ---- word-mask phase tables for the first FB filters ---------------------------------
+    std::vector<uint32_t> mask_off(ES_FMAX + 1, 0);
+    for (uint32_t f = 0; f < ES_FMAX; ++f)
+        mask_off[f + 1] = mask_off[f] + (f < FB ? (uint32_t)align_up((uint64_t)c->q[f] * W, 4) : 0u);
+    std::vector<uint32_t> masks(std::max<uint32_t>(mask_off[ES_FMAX], 4), 0u);
+    for (uint32_t f = 0; f < FB; ++f) {
+        const uint32_t q = c->q[f];
+        uint32_t* P = masks.data() + mask_off[f];
+        for (uint32_t i = 0; i < r0; ++i) {
+            const uint32_t a = mod_q(S0[i], q);
+            const uint32_t wd = i >> 5, bit = 1u << (i & 31u);
+            uint32_t r = a;
+            for (uint32_t ph = 0; ph < q; ++ph) {
+                if (admissible(f, r)) P[(uint64_t)ph * W + wd] |= bit;
+                if (++r == q) r = 0;
+            }
+        }
+    }
+    c->fast_words_mask.assign(mask_off.begin(), mask_off.begin() + FB + 1);
+
+    // ---- arena ----------------------------------------------------------------------------
+    size_t aoff = 0;
+    auto atake = [&](size_t bytes) { size_t o = aoff; aoff = align_up(aoff + bytes, 256); return o; };
+    const size_t a_inst = atake(sizeof(EsInst));
+    const size_t a_small = atake(small_bytes);
+    const size_t a_masks = atake(4ull * masks.size());
+    const size_t a_bits = atake(4ull * std::max<uint32_t>(bit_off[nf], 4));
+    const size_t a_terms = atake(16ull * terms.size());
+    const size_t a_roff = atake(4ull * nr);
+    const size_t a_radix = atake(4ull * nr);
+    c->arena_bytes = aoff;
+    std::vector<unsigned char> img(aoff, 0);
+    memcpy(&img[a_small], small.data(), small_bytes);
+    memcpy(&img[a_masks], masks.data(), 4ull * masks.size());
+    if (bit_off[nf]) memcpy(&img[a_bits], d->allowed, 4ull * bit_off[nf]);
+    for (size_t i = 0; i < terms.size(); ++i) {
+        uint64_t lo = (uint64_t)terms[i], hi = (uint64_t)(terms[i] >> 64);
+        memcpy(&img[a_terms + 16 * i], &lo, 8);
+        memcpy(&img[a_terms + 16 * i + 8], &hi, 8);
+    }
+    memcpy(&img[a_roff], roff.data(), 4ull * nr);
+    memcpy(&img[a_radix], radix.data(), 4ull * nr);
+
+    cudaError_t ce = cudaMalloc(&c->d_arena, aoff);
+    if (ce != cudaSuccess) { es_ctx_destroy(c); return cuda_fail(ce, "cudaMalloc(arena)"); }
+    I.M_lo = (uint64_t)M;
+    I.M_hi = (uint64_t)(M >> 64);
+    I.n_outer = R / r0;
+    I.n_cycles = I.n_outer / r1;
+    I.k = d->k;
+    I.n_rings = nr;
+    I.r0 = r0; I.W = W; I.r1 = r1; I.r2 = r2;
+    I.n_filters = nf;
+    I.F_built = FB;
+    I.sh = sh;
+    I.bsh = bsh;
+    I.tail_mask = (r0 % 32) ? ((1u << (r0 % 32)) - 1u) : 0xffffffffu;
+    I.small_bytes = (uint32_t)small_bytes;
+    for (uint32_t f = 0; f <= ES_FMAX; ++f) I.mask_off[f] = mask_off[f];
+    I.small = c->d_arena + a_small;
+    I.masks = reinterpret_cast<const uint32_t*>(c->d_arena + a_masks);
+    I.allowed = reinterpret_cast<const uint32_t*>(c->d_arena + a_bits);
+    I.ring_terms = reinterpret_cast<const uint64_t*>(c->d_arena + a_terms);
+    I.ring_off = reinterpret_cast<const uint32_t*>(c->d_arena + a_roff);
+    I.radix = reinterpret_cast<const uint32_t*>(c->d_arena + a_radix);
+    memcpy(&img[a_inst], &I, sizeof(EsInst));
+    c->d_inst = reinterpret_cast<EsInst*>(c->d_arena + a_inst);
+    c->table_bytes = aoff;
+
+    ce = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (ce == cudaSuccess) ce = cudaMemcpy(c->d_arena, img.data(), aoff, cudaMemcpyHostToDevice);
+    if (ce == cudaSuccess) ce = cudaEventCreate(&c->ev0);
+    if (ce == cudaSuccess) ce = cudaEventCreate(&c->ev1);
+    if (ce == cudaSuccess) ce = cudaMalloc(&c->d_counts, 8ull * std::max<uint32_t>(nf, 1));
+    if (ce == cudaSuccess) ce = cudaMalloc(&c->d_surv_n, 8ull * 8);
+    if (ce == cudaSuccess) ce = cudaHostAlloc(&c->h_pin, 8ull * 8, cudaHostAllocDefault);
+    if (ce == cudaSuccess) ce = cudaMemset(c->d_counts, 0, 8ull * std::max<uint32_t>(nf, 1));
+    if (ce == cudaSuccess) ce = cudaMemset(c->d_surv_n, 0, 8ull * 8);
+    if (ce != cudaSuccess) { es_ctx_destroy(c); return cuda_fail(ce, "context setup"); }
+    // d_surv_n block: [0] survivor count, [1] unit counter, [2] group found, [3..6] group min
+    c->d_unit = c->d_surv_n + 1;
+    c->d_found = c->d_surv_n + 2;
+    c->d_min = c->d_surv_n + 3;
+    ce = cudaMemset(c->d_found, 0xff, 8);
+    if (ce != cudaSuccess) { es_ctx_destroy(c); return cuda_fail(ce, "context setup"); }
+    int e = es_set_capacity(c, 1u << 20);
+    if (e) { es_ctx_destroy(c); return e; }
+    *out = c;
+    return ES_OK;
+}
+
+int es_ctx_set_tune(es_ctx* c, const es_tune* t) {
+    if (!c || !t) return fail(ES_ERR_ARG, "null argument");
+    if (int e = check_tune(*t)) return e;
+    c->tune = *t;
+    return ES_OK;
+}
+
+int es_ctx_get_tune(const es_ctx* c, es_tune* t) {
+    if (!c || !t) return fail(ES_ERR_ARG, "null argument");
+    *t = c->tune;
+    return ES_OK;
+}
+
+int es_ctx_info(const es_ctx* c, uint64_t* n_outer, uint32_t* r0, uint32_t* n_filters,
+                uint64_t* table_bytes) {
+    if (!c) return fail(ES_ERR_ARG, "null context");
+    if (n_outer) *n_outer = c->h_inst.n_outer;
+    if (r0) *r0 = c->h_inst.r0;
+    if (n_filters) *n_filters = c->h_inst.n_filters;
+    if (table_bytes) *table_bytes = c->table_bytes;
+    return ES_OK;
+}
+
+int es_set_capacity(es_ctx* c, uint64_t cap) {
+    if (!c || cap == 0 || cap > (1ull << 32)) return fail(ES_ERR_ARG, "capacity must be in [1, 2^32]");
+    ES_CUDA(cudaStreamSynchronize(c->stream), "sync");
+    cudaFree(c->d_surv);
+    c->d_surv = nullptr;
+    ES_CUDA(cudaMalloc(&c->d_surv, sizeof(es_survivor) * cap), "cudaMalloc(survivors)");
+    c->surv_cap = cap;
+    return ES_OK;
+}
+
+int es_set_block(es_ctx* c, const uint32_t* tconst, uint32_t n, uint64_t t) {
+    if (!c) return fail(ES_ERR_ARG, "null context");
+    if (n != c->h_inst.n_filters || (n && !tconst))
+        return fail(ES_ERR_ARG, "tconst length must equal the number of filters");
+    for (uint32_t f = 0; f < n; ++f) {
+        if (tconst[f] >= c->q[f]) return fail(ES_ERR_ARG, "tconst[j] must be < q_j");
+        c->tconst[f] = tconst[f];
+    }
+    c->t = t;
+    return ES_OK;
+}
+
+int es_reset_survivors(es_ctx* c) {
+    if (!c) return fail(ES_ERR_ARG, "null context");
+    ES_CUDA(cudaMemsetAsync(c->d_surv_n, 0, 8, c->stream), "memset");
+    ES_CUDA(cudaMemsetAsync(c->d_found, 0xff, 8, c->stream), "memset");
+    return ES_OK;
+}
+
+int es_reset_counts(es_ctx* c) {
+    if (!c) return fail(ES_ERR_ARG, "null context");
+    ES_CUDA(cudaMemsetAsync(c->d_counts, 0, 8ull * std::max<uint32_t>(c->h_inst.n_filters, 1),
+                            c->stream), "memset");
+    return ES_OK;
+}
+
+static int ctx_launch(es_ctx* c, uint64_t ob, uint64_t oe, const uint64_t* d_list) {
+    const EsInst& I = c->h_inst;
+    const es_tune& tn = c->tune;
+    EsLaunch L;
+    memset(&L, 0, sizeof(L));
+    EsItem& it = L.item0;
+    it.inst = c->d_inst;
+    it.tconst = nullptr;
+    it.list = d_list;
+    it.counts = tn.count_stages ? c->d_counts : nullptr;
+    it.t = c->t;
+    it.o_begin = ob;
+    it.o_end = oe;
+    uint64_t n_work;
+    if (d_list) {
+        it.c_begin = it.c_end = 0;
+        n_work = oe - ob;
+    } else {
+        n_work = cycles_of(I, ob, oe, &it.c_begin);
+        it.c_end = it.c_begin + n_work;
+    }
+    const uint64_t per_unit = (uint64_t)tn.threads * tn.strip;
+    it.unit_begin = 0;
+    it.n_units = (n_work + per_unit - 1) / per_unit;
+    it.group = 0;
+    it.inst_id = 0;
+    const uint32_t F = std::min<uint32_t>(tn.mask_filters, std::max<uint32_t>(I.n_filters, 1));
+    const SmemPlan sp = plan_smem((uint32_t)I.small_bytes, I.n_filters, tn, fast_need(c, tn.layout, F));
+    fast_prefix(c, tn.layout, F, sp.fast_words_cap, &it.n_sm, &it.sm_fast_words);
+    L.items = nullptr;
+    L.n_items = 1;
+    L.threads = tn.threads;
+    L.strip = tn.strip;
+    L.mask_filters = tn.mask_filters;
+    L.total_units = it.n_units;
+    L.cycles_per_unit = per_unit;
+    L.unit_counter = c->d_unit;
+    L.surv = c->d_surv;
+    L.surv_n = c->d_surv_n;
+    L.surv_cap = c->surv_cap;
+    L.group_found = nullptr;
+    L.smem_bytes = sp.bytes;
+    L.tconst_off = sp.tconst_off;
+    L.fast_off = sp.fast_off;
+    L.cnt_off = sp.cnt_off;
+    memcpy(L.tconst0, c->tconst, 4ull * I.n_filters);
+    if (it.n_units == 0) return ES_OK;
+    int grid = 0;
+    if (int e = grid_for(tn.layout, tn.count_stages, tn, sp.bytes, it.n_units, &grid)) return e;
+    ES_CUDA(cudaMemsetAsync(c->d_unit, 0, 8, c->stream), "memset");
+    int e = es_launch_scan(L, (int)tn.layout, (int)tn.count_stages, grid, c->stream);
+    if (e) return cuda_fail((cudaError_t)e, "scan launch");
+    c->launched = true;
+    return ES_OK;
+}
+
+int es_launch(es_ctx* c, uint64_t ostart, uint64_t ocount) {
+    if (!c) return fail(ES_ERR_ARG, "null context");
+    if (ostart > c->h_inst.n_outer || ocount > c->h_inst.n_outer - ostart)
+        return fail(ES_ERR_RANGE, "outer range outside [0, R/r0)");
+    return ctx_launch(c, ostart, ostart + ocount, nullptr);
+}
+
+int es_launch_list(es_ctx* c, const uint64_t* outer, uint64_t n) {
+    if (!c || (n && !outer)) return fail(ES_ERR_ARG, "null argument");
+    for (uint64_t i = 0; i < n; ++i)
+        if (outer[i] >= c->h_inst.n_outer) return fail(ES_ERR_RANGE, "outer index outside [0, R/r0)");
+    if (n == 0) return ES_OK;
+    ES_CUDA(cudaStreamSynchronize(c->stream), "sync");
+    if (n > c->list_cap) {
+        cudaFree(c->d_list);
+        c->d_list = nullptr;
+        ES_CUDA(cudaMalloc(&c->d_list, 8ull * n), "cudaMalloc(list)");
+        c->list_cap = n;
+    }
+    ES_CUDA(cudaMemcpy(c->d_list, outer, 8ull * n, cudaMemcpyHostToDevice), "copy list");
+    return ctx_launch(c, 0, n, c->d_list);
+}
+
+int es_sync(es_ctx* c) {
+    if (!c) return fail(ES_ERR_ARG, "null context");
+    ES_CUDA(cudaStreamSynchronize(c->stream), "kernel execution");
+    return ES_OK;
+}
+
+int es_survivor_count(es_ctx* c, uint64_t* n) {
+    if (!c || !n) return fail(ES_ERR_ARG, "null argument");
+    ES_CUDA(cudaMemcpyAsync(c->h_pin, c->d_surv_n, 8, cudaMemcpyDeviceToHost, c->stream), "copy");
+    ES_CUDA(cudaStreamSynchronize(c->stream), "kernel execution");
+    *n = c->h_pin[0];
+    return ES_OK;
+}
+
+int es_read_survivor_records(es_ctx* c, es_survivor* out, uint64_t cap, uint64_t* n) {
+    if (!c || !n) return fail(ES_ERR_ARG, "null argument");
+    uint64_t cnt = 0;
+    if (int e = es_survivor_count(c, &cnt)) return e;
+    *n = cnt;
+    if (cnt > c->surv_cap)
+        return fail(ES_ERR_OVERFLOW, "survivor buffer overflow (" + std::to_string(cnt) + " > " +
+                                         std::to_string(c->surv_cap) + "); raise max_survivors");
+    if (cnt > cap) return fail(ES_ERR_OVERFLOW, "output buffer smaller than the survivor count");
+    if (cnt) ES_CUDA(cudaMemcpy(out, c->d_surv, sizeof(es_survivor) * cnt, cudaMemcpyDeviceToHost), "copy");
+    return ES_OK;
+}
+
+int es_read_survivors(es_ctx* c, uint64_t* idx_out, uint64_t cap, uint64_t* n) {
+    if (!c || !n) return fail(ES_ERR_ARG, "null argument");
+    uint64_t cnt = 0;
+    if (int e = es_survivor_count(c, &cnt)) return e;
+    *n = cnt;
+    if (cnt > c->surv_cap)
+        return fail(ES_ERR_OVERFLOW, "survivor buffer overflow (" + std::to_string(cnt) + " > " +
+                                         std::to_string(c->surv_cap) + "); raise max_survivors");
+    if (cnt > cap) return fail(ES_ERR_OVERFLOW, "output buffer smaller than the survivor count");
+    if (!cnt) return ES_OK;
+    std::vector<es_survivor> tmp(cnt);
+    ES_CUDA(cudaMemcpy(tmp.data(), c->d_surv, sizeof(es_survivor) * cnt, cudaMemcpyDeviceToHost), "copy");
+    for (uint64_t i = 0; i < cnt; ++i) idx_out[i] = tmp[i].idx;
+    return ES_OK;
+}
+
+int es_stage_counts(es_ctx* c, uint64_t* counts, uint32_t n) {
+    if (!c || (n && !counts)) return fail(ES_ERR_ARG, "null argument");
+    if (n != c->h_inst.n_filters) return fail(ES_ERR_ARG, "counts length must equal the filter count");
+    ES_CUDA(cudaStreamSynchronize(c->stream), "kernel execution");
+    if (n) ES_CUDA(cudaMemcpy(counts, c->d_counts, 8ull * n, cudaMemcpyDeviceToHost), "copy");
+    return ES_OK;
+}
+
+int es_min_survivor(es_ctx* c, int* found, uint64_t* t, uint64_t* s_lo, uint64_t* s_hi) {
+    if (!c || !found) return fail(ES_ERR_ARG, "null argument");
+    int e = es_launch_min(c->d_surv, c->d_surv_n, c->surv_cap, nullptr, 1, c->d_min, c->stream);
+    if (e) return cuda_fail((cudaError_t)e, "min launch");
+    ES_CUDA(cudaMemcpyAsync(c->h_pin, c->d_min, 32, cudaMemcpyDeviceToHost, c->stream), "copy");
+    ES_CUDA(cudaStreamSynchronize(c->stream), "kernel execution");
+    *found = (int)c->h_pin[0];
+    if (t) *t = c->h_pin[1];
+    if (s_lo) *s_lo = c->h_pin[2];
+    if (s_hi) *s_hi = c->h_pin[3];
+    return ES_OK;
+}
+
+int es_launch_timed(es_ctx* c, uint64_t ostart, uint64_t ocount, float* ms) {
+    if (!c) return fail(ES_ERR_ARG, "null context");
+    ES_CUDA(cudaEventRecord(c->ev0, c->stream), "event");
+    if (int e = es_launch(c, ostart, ocount)) return e;
+    ES_CUDA(cudaEventRecord(c->ev1, c->stream), "event");
+    ES_CUDA(cudaEventSynchronize(c->ev1), "kernel execution");
+    float v = 0.f;
+    ES_CUDA(cudaEventElapsedTime(&v, c->ev0, c->ev1), "event");
+    if (ms) *ms = v;
+    return ES_OK;
+}
+
+// ---------------------------------------------------------------------------------------
+int es_batch_destroy(es_batch* b) {
+    if (!b) return ES_OK;
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    cudaFree(b->d_items);
+    cudaFree(b->d_tconst);
+    cudaFree(b->d_counts);
+    cudaFree(b->d_surv);
+    cudaFree(b->d_surv_n);
+    if (b->ev0) cudaEventDestroy(b->ev0);
+    if (b->ev1) cudaEventDestroy(b->ev1);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+    return ES_OK;
+}
+
+int es_batch_create(es_ctx* const* ctxs, uint32_t n_ctx, const es_batch_item* items,
+                    uint32_t n_items, const es_tune* tune_in, es_batch** out) {
+    if (!ctxs || !items || !out || n_ctx == 0 || n_items == 0)
+        return fail(ES_ERR_ARG, "empty batch");
+    *out = nullptr;
+    es_tune tune = tune_in ? *tune_in : ctxs[0]->tune;
+    if (int e = check_tune(tune)) return e;
+    if (int e = device_facts()) return e;
+    es_batch* b = new (std::nothrow) es_batch();
+    if (!b) return fail(ES_ERR_NOMEM, "host allocation");
+    b->tune = tune;
+    b->ctxs.assign(ctxs, ctxs + n_ctx);
+    // launch-wide smem plan: the largest small block / filter count, one fast-table budget
+    uint32_t small_max = 0, nf_max = 1, need_max = 0;
+    for (uint32_t i = 0; i < n_ctx; ++i) {
+        const es_ctx* c = ctxs[i];
+        if (!c) { es_batch_destroy(b); return fail(ES_ERR_ARG, "null context in batch"); }
+        small_max = std::max<uint32_t>(small_max, c->h_inst.small_bytes);
+        nf_max = std::max<uint32_t>(nf_max, c->h_inst.n_filters);
+        const uint32_t F = std::min<uint32_t>(tune.mask_filters, std::max<uint32_t>(c->h_inst.n_filters, 1));
+        need_max = std::max<uint32_t>(need_max, fast_need(c, tune.layout, F));
+    }
+    const SmemPlan sp = plan_smem(small_max, nf_max, tune, need_max);
+    const uint64_t per_unit = (uint64_t)tune.threads * tune.strip;
+    std::vector<uint32_t> h_tc;
+    b->h_items.resize(n_items);
+    b->count_off.resize(n_items);
+    uint64_t units = 0, cwords = 0;
+    uint32_t max_group = 0;
+    for (uint32_t i = 0; i < n_items; ++i) {
+        const es_batch_item& s = items[i];
+        if (s.ctx_index >= n_ctx) { es_batch_destroy(b); return fail(ES_ERR_ARG, "item ctx_index out of range"); }
+        if (s.group >= n_items) { es_batch_destroy(b); return fail(ES_ERR_ARG, "item group must be < n_items"); }
+        const es_ctx* c = ctxs[s.ctx_index];
+        const EsInst& I = c->h_inst;
+        if (s.o_begin > s.o_end || s.o_end > I.n_outer) {
+            es_batch_destroy(b);
+            return fail(ES_ERR_RANGE, "item outer range outside [0, R/r0)");
+        }
+        EsItem& it = b->h_items[i];
+        memset(&it, 0, sizeof(it));
+        it.inst = c->d_inst;
+        it.list = nullptr;
+        it.t = s.t;
+        it.o_begin = s.o_begin;
+        it.o_end = s.o_end;
+        const uint64_t ncyc = s.o_end > s.o_begin ? cycles_of(I, s.o_begin, s.o_end, &it.c_begin) : 0;
+        it.c_end = it.c_begin + ncyc;
+        it.unit_begin = units;
+        it.n_units = (ncyc + per_unit - 1) / per_unit;
+        units += it.n_units;
+        it.group = s.group;
+        it.inst_id = s.ctx_index;
+        const uint32_t F = std::min<uint32_t>(tune.mask_filters, std::max<uint32_t>(I.n_filters, 1));
+        fast_prefix(c, tune.layout, F, sp.fast_words_cap, &it.n_sm, &it.sm_fast_words);
+        // per-block constants tconst[j] = (t mod q)(M mod q) mod q
+        it.tconst = reinterpret_cast<const uint32_t*>((uintptr_t)h_tc.size());  // patched below
+        for (uint32_t f = 0; f < I.n_filters; ++f) {
+            const uint64_t q = c->q[f];
+            const uint64_t mq = (uint64_t)(c->M % q);
+            h_tc.push_back((uint32_t)((s.t % q) * mq % q));
+        }
+        while (h_tc.size() % 4) h_tc.push_back(0);
+        b->count_off[i] = cwords;
+        cwords += std::max<uint32_t>(I.n_filters, 1);
+        max_group = std::max<uint32_t>(max_group, s.group);
+    }
+    b->n_groups = max_group + 1;
+    b->counts_words = cwords;
+    cudaError_t ce = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+    if (ce == cudaSuccess) ce = cudaEventCreate(&b->ev0);
+    if (ce == cudaSuccess) ce = cudaEventCreate(&b->ev1);
+    if (ce == cudaSuccess) ce = cudaMalloc(&b->d_items, sizeof(EsItem) * n_items);
+    if (ce == cudaSuccess) ce = cudaMalloc(&b->d_tconst, 4ull * std::max<size_t>(h_tc.size(), 4));
+    if (ce == cudaSuccess) ce = cudaMalloc(&b->d_counts, 8ull * cwords);
+    // scalars: [0] survivor count, [1] unit counter, then group_found[G], group_min[4G]
+    if (ce == cudaSuccess) ce = cudaMalloc(&b->d_surv_n, 8ull * (2 + 5ull * b->n_groups));
+    b->surv_cap = ctxs[0]->surv_cap;
+    if (ce == cudaSuccess) ce = cudaMalloc(&b->d_surv, sizeof(es_survivor) * b->surv_cap);
+    if (ce != cudaSuccess) { es_batch_destroy(b); return cuda_fail(ce, "batch setup"); }
+    b->d_unit = b->d_surv_n + 1;
+    b->d_found = b->d_surv_n + 2;
+    b->d_min = b->d_surv_n + 2 + b->n_groups;
+    for (uint32_t i = 0; i < n_items; ++i) {
+        EsItem& it = b->h_items[i];
+        it.tconst = b->d_tconst + (uintptr_t)it.tconst;
+        it.counts = tune.count_stages ? b->d_counts + b->count_off[i] : nullptr;
+    }
+    ce = cudaMemcpy(b->d_items, b->h_items.data(), sizeof(EsItem) * n_items, cudaMemcpyHostToDevice);
+    if (ce == cudaSuccess && !h_tc.empty())
+        ce = cudaMemcpy(b->d_tconst, h_tc.data(), 4ull * h_tc.size(), cudaMemcpyHostToDevice);
+    if (ce != cudaSuccess) { es_batch_destroy(b); return cuda_fail(ce, "batch upload"); }
+
+    EsLaunch& L = b->L;
+    memset(&L, 0, sizeof(L));
+    L.items = b->d_items;
+    L.n_items = n_items;
+    L.threads = tune.threads;
+    L.strip = tune.strip;
+    L.mask_filters = tune.mask_filters;
+    L.total_units = units;
+    L.cycles_per_unit = per_unit;
+    L.unit_counter = b->d_unit;
+    L.surv = b->d_surv;
+    L.surv_n = b->d_surv_n;
+    L.surv_cap = b->surv_cap;
+    L.group_found = b->d_found;
+    L.smem_bytes = sp.bytes;
+    L.tconst_off = sp.tconst_off;
+    L.fast_off = sp.fast_off;
+    L.cnt_off = sp.cnt_off;
+    if (int e = grid_for(tune.layout, tune.count_stages, tune, sp.bytes, std::max<uint64_t>(units, 1), &b->grid)) {
+        es_batch_destroy(b);
+        return e;
+    }
+    *out = b;
+    return ES_OK;
+}
+
+static int batch_enqueue(es_batch* b) {
+    ES_CUDA(cudaMemsetAsync(b->d_surv_n, 0, 16, b->stream), "memset");
+    ES_CUDA(cudaMemsetAsync(b->d_found, 0xff, 8ull * b->n_groups, b->stream), "memset");
+    if (b->counts_words)
+        ES_CUDA(cudaMemsetAsync(b->d_counts, 0, 8ull * b->counts_words, b->stream), "memset");
+    if (b->L.total_units) {
+        int e = es_launch_scan(b->L, (int)b->tune.layout, (int)b->tune.count_stages, b->grid, b->stream);
+        if (e) return cuda_fail((cudaError_t)e, "scan launch");
+    }
+    int e = es_launch_min(b->d_surv, b->d_surv_n, b->surv_cap, b->d_items, b->n_groups, b->d_min, b->stream);
+    if (e) return cuda_fail((cudaError_t)e, "min launch");
+    return ES_OK;
+}
+
+int es_batch_run(es_batch* b, int use_graph) {
+    if (!b) return fail(ES_ERR_ARG, "null batch");
+    ES_CUDA(cudaEventRecord(b->ev0, b->stream), "event");
+    if (use_graph) {
+        if (!b->exec) {
+            ES_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal), "capture");
+            int e = batch_enqueue(b);
+            cudaGraph_t g = nullptr;
+            cudaError_t ce = cudaStreamEndCapture(b->stream, &g);
+            if (e) { if (g) cudaGraphDestroy(g); return e; }
+            if (ce != cudaSuccess) return cuda_fail(ce, "end capture");
+            b->graph = g;
+            ES_CUDA(cudaGraphInstantiate(&b->exec, g, 0), "graph instantiate");
+        }
+        ES_CUDA(cudaGraphLaunch(b->exec, b->stream), "graph launch");
+    } else {
+        if (int e = batch_enqueue(b)) return e;
+    }
+    ES_CUDA(cudaEventRecord(b->ev1, b->stream), "event");
+    b->ran = true;
+    return ES_OK;
+}
+
+int es_batch_sync(es_batch* b, float* ms) {
+    if (!b) return fail(ES_ERR_ARG, "null batch");
+    ES_CUDA(cudaStreamSynchronize(b->stream), "kernel execution");
+    if (ms) {
+        float v = 0.f;
+        if (b->ran) ES_CUDA(cudaEventElapsedTime(&v, b->ev0, b->ev1), "event");
+        *ms = v;
+    }
+    return ES_OK;
+}
+
+int es_batch_group_min(es_batch* b, uint32_t group, int* found, uint64_t* t, uint64_t* s_lo,
+                       uint64_t* s_hi) {
+    if (!b || !found) return fail(ES_ERR_ARG, "null argument");
+    if (group >= b->n_groups) return fail(ES_ERR_ARG, "group out of range");
+    if (!b->ran) return fail(ES_ERR_STATE, "batch has not run");
+    ES_CUDA(cudaStreamSynchronize(b->stream), "kernel execution");
+    unsigned long long v[4];
+    ES_CUDA(cudaMemcpy(v, b->d_min + 4ull * group, 32, cudaMemcpyDeviceToHost), "copy");
+    *found = (int)v[0];
+    if (t) *t = v[1];
+    if (s_lo) *s_lo = v[2];
+    if (s_hi) *s_hi = v[3];
+    return ES_OK;
+}
+
+int es_batch_item_counts(es_batch* b, uint32_t item, uint64_t* counts, uint32_t n) {
+    if (!b || (n && !counts)) return fail(ES_ERR_ARG, "null argument");
+    if (item >= b->h_items.size()) return fail(ES_ERR_ARG, "item out of range");
+    const uint32_t nf = b->ctxs[b->h_items[item].inst_id]->h_inst.n_filters;
+    if (n != nf) return fail(ES_ERR_ARG, "counts length must equal the item's filter count");
+    if (!b->ran) return fail(ES_ERR_STATE, "batch has not run");
+    ES_CUDA(cudaStreamSynchronize(b->stream), "kernel execution");
+    if (n) ES_CUDA(cudaMemcpy(counts, b->d_counts + b->count_off[item], 8ull * n, cudaMemcpyDeviceToHost), "copy");
+    return ES_OK;
+}
+
+int es_batch_survivors(es_batch* b, es_survivor* out, uint64_t cap, uint64_t* n) {
+    if (!b || !n) return fail(ES_ERR_ARG, "null argument");
+    if (!b->ran) return fail(ES_ERR_STATE, "batch has not run");
+    ES_CUDA(cudaStreamSynchronize(b->stream), "kernel execution");
+    unsigned long long cnt = 0;
+    ES_CUDA(cudaMemcpy(&cnt, b->d_surv_n, 8, cudaMemcpyDeviceToHost), "copy");
+    *n = cnt;
+    if (cnt > b->surv_cap) return fail(ES_ERR_OVERFLOW, "survivor buffer overflow");
+    if (cnt > cap) return fail(ES_ERR_OVERFLOW, "output buffer smaller than the survivor count");
+    if (cnt) ES_CUDA(cudaMemcpy(out, b->d_surv, sizeof(es_survivor) * cnt, cudaMemcpyDeviceToHost), "copy");
+    return ES_OK;
+}
+
+int es_int_peak(double* ops_per_s, double* ms_out) {
+    if (int e = device_facts()) return e;
+    unsigned long long* sink = nullptr;
+    ES_CUDA(cudaMalloc(&sink, 8), "cudaMalloc");
+    cudaEvent_t a, z;
+    cudaEventCreate(&a);
+    cudaEventCreate(&z);
+    const int threads = 256, grid = g_dev.sms * 8, iters = 4096;
+    float best = 1e30f;
+    for (int rep = 0; rep < 4; ++rep) {
+        cudaEventRecord(a);
+        int e = es_launch_int_peak(sink, grid, threads, iters, nullptr);
+        cudaEventRecord(z);
+        cudaError_t ce = cudaEventSynchronize(z);
+        if (e || ce != cudaSuccess) {
+            cudaFree(sink);
+            return cuda_fail(e ? (cudaError_t)e : ce, "int peak kernel");
+        }
+        float v = 0.f;
+        cudaEventElapsedTime(&v, a, z);
+        if (rep > 0 && v < best) best = v;
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(z);
+    cudaFree(sink);
+    const double ops = (double)grid * threads * (double)iters * 256.0;
+    if (ops_per_s) *ops_per_s = ops / (best * 1e-3);
+    if (ms_out) *ms_out = best;
+    return ES_OK;
+}
+
+}  // extern "C"

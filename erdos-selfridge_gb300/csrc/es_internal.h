@@ -1,0 +1,112 @@
+// Internal layout shared by the host table builder (es_abi.cu) and the kernels (es_scan.cu).
+//
+// Data layout in HBM (one arena per plan context, uploaded once):
+//   small block   contiguous tables staged verbatim into shared memory by every CTA:
+//                   T1[r1]      ring-1 terms (128-bit)                      16 B each
+//                   TQ1[r1][8]  ring-1 terms mod q_f, f < 8                  32 B each
+//                   D2[r2]      ring-2 step deltas term2[d+1]-term2[d] mod M 16 B each
+//                   DQ2[r2][8]  those deltas mod q_f                        32 B each
+//                   S0[r0]      inner-ring terms sorted ascending            16 B each
+//                   K0[r0]      top-32-bit keys of S0 (carry-split search)    4 B each
+//                   I0[r0]      original inner digit of each sorted slot      4 B each
+//                   Q0[8][r0]   S0 mod q_f (scalar layout)                    4 B each
+//                   BK[1025]    carry-split bucket starts over key top bits   2 B each
+//                   FC[nf]      per-filter constants (EsFilterC)             32 B each
+//   fast tables   for the first F_built filters: word-mask phase tables
+//                   P_f[phi][w] bit i = admissible((phi + S0[32w+i]) mod q_f), q_f x W words
+//   bit tables    every filter's packed admissible-residue bits (ceil(q/32) words)
+//   ring terms    all rings' 128-bit terms (decode of rings >= 2 at strip starts)
+#pragma once
+#include <stdint.h>
+
+#define ES_FMAX 8
+#define ES_NBUCKET 1024
+#define ES_MAX_RINGS 64
+#define ES_MAX_FILTERS 192   // pi(1024) = 172 residual primes at most
+
+struct EsFilterC {
+    uint32_t q;      // modulus p^t_p (< 2^20)
+    uint32_t corr;   // (q - M mod q) mod q: residue correction when a sum wraps mod M
+    uint32_t w1;     // 2^32 mod q
+    uint32_t w2;     // 2^64 mod q
+    uint32_t w3;     // 2^96 mod q
+    uint32_t off;    // word offset of this filter's bit table
+    uint64_t rcp;    // floor(2^64 / q): Barrett reciprocal for 64-bit residues
+};
+
+struct EsInst {
+    uint64_t M_lo, M_hi;
+    uint64_t n_outer;     // R / r0 outer indices per block
+    uint64_t n_cycles;    // n_outer / r1 ring-1 cycles per block
+    uint32_t k;
+    uint32_t n_rings;     // >= 3 after padding with radix-1 rings
+    uint32_t r0, W, r1, r2;
+    uint32_t n_filters;
+    uint32_t F_built;     // filters with word-mask tables (<= ES_FMAX)
+    uint32_t sh;          // key shift: keys = value >> sh (top 32 bits of M's width)
+    uint32_t bsh;         // bucket shift: bucket = key >> bsh
+    uint32_t tail_mask;   // valid bits of the last inner word
+    uint32_t small_bytes; // size of the small block (multiple of 16)
+    // byte offsets inside the small block
+    uint32_t o_T1, o_TQ1, o_D2, o_DQ2, o_S0, o_K0, o_I0, o_Q0, o_BK, o_FC;
+    // word offsets of the fast (word-mask) tables, F_built + 1 entries (prefix sums)
+    uint32_t mask_off[ES_FMAX + 1];
+    uint32_t pad0;
+    const unsigned char* small;      // device copy of the small block
+    const uint32_t* masks;           // word-mask tables
+    const uint32_t* allowed;         // bit tables of all filters
+    const uint64_t* ring_terms;      // [sum radix][2] lo,hi
+    const uint32_t* ring_off;        // [n_rings]
+    const uint32_t* radix;           // [n_rings]
+};
+
+// One work item of a launch, device-resident.
+struct EsItem {
+    const EsInst* inst;      // device pointer
+    const uint32_t* tconst;  // [n_filters] per-block residue constants (device)
+    const uint64_t* list;    // explicit outer-index list or nullptr (range mode)
+    unsigned long long* counts;  // [n_filters] stage counts (device) or nullptr
+    uint64_t t;
+    uint64_t o_begin, o_end; // range mode: outer range; list mode: list index range
+    uint64_t c_begin, c_end; // range mode: cycle range covering the outer range
+    uint64_t unit_begin;     // first global unit of this item
+    uint64_t n_units;
+    uint32_t group;
+    uint32_t inst_id;        // distinct per plan context within a launch
+    uint32_t n_sm;           // fast tables of filters [0, n_sm) are staged in smem
+    uint32_t sm_fast_words;  // words of fast tables staged
+};
+
+struct EsLaunch {
+    const EsItem* items;
+    uint32_t n_items;
+    uint32_t threads;
+    uint32_t strip;
+    uint32_t mask_filters;   // F requested (template F is the rounded-up instance)
+    uint64_t total_units;
+    uint64_t cycles_per_unit;      // threads * strip
+    unsigned long long* unit_counter;
+    struct es_survivor* surv;
+    unsigned long long* surv_n;
+    uint64_t surv_cap;
+    unsigned long long* group_found;  // per group: least block with a good survivor
+    uint32_t smem_bytes;              // dynamic shared memory of the launch
+    uint32_t tconst_off;              // byte offset of the staged tconst in smem
+    uint32_t fast_off;                // byte offset of the staged fast tables in smem
+    uint32_t cnt_off;                 // byte offset of the per-stage counters in smem
+    uint32_t pad1;
+    // single-plan launches carry their one item and block constants by value
+    EsItem item0;
+    uint32_t tconst0[ES_MAX_FILTERS];
+};
+
+// Host-side launchers implemented in es_scan.cu (return a cudaError_t value).
+int es_scan_prepare(int smem_optin_bytes);
+int es_scan_occupancy(int layout, int count, uint32_t mask_filters, int threads, int smem_bytes,
+                      int* ctas_per_sm);
+int es_launch_scan(const EsLaunch& L, int layout, int count, int grid, void* stream);
+// group_min: [n_groups][4] = {found, t, s_lo, s_hi}; items == nullptr means one group (0)
+int es_launch_min(const struct es_survivor* surv, const unsigned long long* surv_n,
+                  uint64_t cap, const EsItem* items, uint32_t n_groups,
+                  unsigned long long* group_min, void* stream);
+int es_launch_int_peak(unsigned long long* sink, int grid, int threads, int iters, void* stream);

@@ -1,0 +1,349 @@
+#!/usr/bin/env python3
+"""GB300 (sm_103a) engine for the Erdős–Selfridge CRT-wheel sieve: a drop-in for the engine
+module that harness/run_k.py, harness/run_k_masks.py and harness/replay_release.py drive.
+
+Usage from the reference harness (no code change there):
+
+    PYTHONPATH=<this directory> ES_ENGINE=es_gb300 python harness/run_k.py 300 --max-blocks 1
+
+Module surface (sieve/gpu_sieve_v9.py): ``Plan``, ``GpuSieve``, ``TUNABLES``, ``plan_wheel``,
+``order_filters``, ``partial_residues``, ``partial_count``, ``free_vram_mib``, ``load_known``
+and ``main`` (same CLI and JSON line).  ``GpuSieve`` keeps every attribute the drivers touch
+(harness/run_k.py:85-124): ``rest_q``, ``rest_Mmodq``, ``tconst_h``, ``tconst.set``, ``r0``,
+``R_outer``, ``ochunk``, ``chunk``, ``out_n.fill/get``, ``out[:n].get()``, ``out_cap``,
+``residues_checked``, ``launches``, ``_launch(ostart, ocount)``, ``scan_block(t)``,
+``search(max_blocks, log)`` and ``mask_mode``.
+
+Compute runs only in libes_gb300.so (hand-written CUDA for sm_103a) through ctypes; there is no
+CPU fallback.  The host re-verifies every survivor of the concluding block with an exact
+Kummer test, as the reference does with its frozen referee (sieve/gpu_sieve_v9.py:551-557).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import signal
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+if HERE not in sys.path:
+    sys.path.insert(0, HERE)
+
+import es_native as N  # noqa: E402
+from es_plan import (MAX_M_BITS, is_admissible, order_filters, partial_count,  # noqa: E402,F401
+                     partial_residues, plan_wheel, primes_upto)
+from es_plan import Plan as _PlanBase  # noqa: E402
+from es_plan import TUNABLES as _PLAN_TUNABLES  # noqa: E402
+
+# Engine tunables on top of the planner's (sieve/gpu_sieve_v9.py:98-120).  Launch shape and
+# table layout never change which candidates pass.
+TUNABLES = dict(_PLAN_TUNABLES)
+TUNABLES.update({
+    "chunk_log2": 34,        # positions per _launch chunk issued by scan_block
+    "layout": "wordmask",    # "wordmask" | "scalar"
+    "strip": 4,              # ring-1 cycles per thread per work unit
+    "smem_kb": 200,          # shared-memory budget for staged tables
+    "ctas_per_sm": 2,
+    "count_stages": 1,       # per-filter-stage pass counts
+    "search_batch_log2": 34, # positions per multi-block search launch
+})
+
+
+SEARCH_MAX_BLOCKS = 1024   # block items per multi-block search launch
+
+
+class Plan(_PlanBase):
+    """The reference Plan (sieve/gpu_sieve_v9.py:344-413) with this engine's TUNABLES defaults."""
+
+    def __init__(self, k: int, tun: dict | None = None, wheel=None, filter_order=None):
+        super().__init__(k, dict(TUNABLES, **(tun or {})), wheel, filter_order)
+
+
+def _tune_from(tun: dict) -> N.Tune:
+    layout = tun.get("layout", "wordmask")
+    return N.make_tune(layout=N.LAYOUT_SCALAR if layout == "scalar" else N.LAYOUT_WORDMASK,
+                       mask_filters=max(1, min(N.MAX_MASK_FILTERS, int(tun.get("fast_filters", 4)))),
+                       threads=int(tun.get("threads", 256)), strip=int(tun.get("strip", 4)),
+                       smem_kb=int(tun.get("smem_kb", 200)), ctas_per_sm=int(tun.get("ctas_per_sm", 2)),
+                       count_stages=int(tun.get("count_stages", 1)))
+
+
+class _Tconst:
+    """Stand-in for the CuPy tconst array: ``.set(host_array)`` uploads block constants."""
+
+    def __init__(self, sieve: "GpuSieve"):
+        self._s = sieve
+
+    def set(self, arr) -> None:
+        self._s._set_tconst(np.asarray(arr, dtype=np.uint32))
+
+
+class _OutN:
+    """Stand-in for the CuPy survivor counter: ``fill(0)`` resets, ``get()[0]`` syncs + reads."""
+
+    def __init__(self, sieve: "GpuSieve"):
+        self._s = sieve
+
+    def fill(self, v) -> None:
+        if int(v) != 0:
+            raise ValueError("only fill(0) is supported")
+        self._s.ctx.reset()
+
+    def get(self) -> np.ndarray:
+        return np.array([self._s.ctx.count()], dtype=np.uint64)
+
+
+class _OutSlice:
+    def __init__(self, sieve: "GpuSieve", sl: slice):
+        self._s, self._sl = sieve, sl
+
+    def get(self) -> np.ndarray:
+        return self._s.ctx.survivors()[self._sl]
+
+
+class _Out:
+    """Stand-in for the CuPy survivor buffer: ``out[:n].get()`` returns block-relative indices."""
+
+    def __init__(self, sieve: "GpuSieve"):
+        self._s = sieve
+
+    def __getitem__(self, sl) -> _OutSlice:
+        if not isinstance(sl, slice):
+            raise TypeError("index the survivor buffer with a slice")
+        return _OutSlice(self._s, sl)
+
+
+class GpuSieve:
+    """One plan resident on the GPU with the reference GpuSieve surface (sieve/gpu_sieve_v9.py:425-568)."""
+
+    def __init__(self, plan: Plan, tune: N.Tune | None = None):
+        self.plan = plan
+        P = plan
+        self.w = len(P.wheel)
+        self.rest_q = [P.info[p][0] for p in P.rest]
+        self.rest_Mmodq = [P.M % q for q in self.rest_q]
+        self.nrest = len(P.rest)
+        self.tconst_h = np.zeros(max(1, self.nrest), dtype=np.uint32)
+        self.r0 = P.radix[0] if P.radix else 1
+        self.n_fast = max(0, min(int(P.tun.get("fast_filters", 4)), self.nrest))
+        self.tune = tune if tune is not None else _tune_from(P.tun)
+        t0 = time.time()
+        self.ctx = N.Context(P, self.tune, capacity=int(P.tun["max_survivors"]))
+        self.compile_s = time.time() - t0          # table build + upload (no run-time compile)
+        self.out_cap = int(P.tun["max_survivors"])
+        self.threads = int(self.tune.threads)
+        self.chunk = 1 << int(P.tun.get("chunk_log2", 34))
+        self.R_outer = P.R // self.r0
+        assert self.R_outer == self.ctx.n_outer
+        self.ochunk = max(1, self.chunk // self.r0)
+        self.launches = 0
+        self.residues_checked = 0
+        self.mask_mode = "wordmask-gb300" if self.tune.layout == N.LAYOUT_WORDMASK else "scalar-gb300"
+        self.tconst = _Tconst(self)
+        self.out_n = _OutN(self)
+        self.out = _Out(self)
+        self._block = 0
+        self._set_tconst(self.tconst_h)
+
+    # ---------------------------------------------------------------- device plumbing
+    def _block_from_tconst(self, tc: np.ndarray) -> int:
+        """Recover t from tconst when the caller only uploads constants (run_k.py path).
+
+        tconst_j = t*M mod q_j, so t mod q_j is known wherever M is invertible mod q_j; CRT over
+        those filters gives t modulo their product, exact for every practical block index."""
+        t_mod, mod = 0, 1
+        for j, q in enumerate(self.rest_q):
+            m = self.rest_Mmodq[j]
+            if math.gcd(m, q) != 1:
+                continue
+            r = (int(tc[j]) * pow(m, -1, q)) % q
+            g = math.gcd(mod, q)
+            if g != 1:
+                continue
+            # combine t = t_mod (mod mod) with t = r (mod q)
+            k = ((r - t_mod) * pow(mod, -1, q)) % q
+            t_mod += mod * k
+            mod *= q
+            if mod > (1 << 64):
+                break
+        return t_mod
+
+    def _set_tconst(self, tc: np.ndarray) -> None:
+        tc = np.ascontiguousarray(tc[:max(self.nrest, 1)], dtype=np.uint32)
+        t = self._block if np.array_equal(tc[:self.nrest], N.tconst_for(self.plan, self._block)[:self.nrest]) \
+            else self._block_from_tconst(tc)
+        self.ctx.set_block(t, tc[:self.nrest] if self.nrest else np.zeros(0, dtype=np.uint32))
+
+    def _launch(self, ostart: int, ocount: int) -> None:
+        """ostart/ocount are OUTER indices; each covers r0 positions (asynchronous)."""
+        self.ctx.launch(int(ostart), int(ocount))
+        self.launches += 1
+
+    # ---------------------------------------------------------------- block scans
+    def scan_block(self, t: int) -> list[int]:
+        """Every position of block t; one device sync per block (sieve/gpu_sieve_v9.py:508-525)."""
+        self._block = int(t)
+        self.tconst_h[:] = N.tconst_for(self.plan, t)[:self.tconst_h.size]
+        self.tconst.set(self.tconst_h)
+        self.out_n.fill(0)
+        ostart = 0
+        while ostart < self.R_outer:
+            ocount = min(self.ochunk, self.R_outer - ostart)
+            self._launch(ostart, ocount)
+            self.residues_checked += ocount * self.r0
+            ostart += ocount
+        n = int(self.out_n.get()[0])
+        if n > self.out_cap:
+            return self._scan_block_chunked(t)
+        return [int(x) for x in self.out[:n].get()] if n else []
+
+    def _scan_block_chunked(self, t: int) -> list[int]:
+        """Per-launch drain, used only when a block overflows the survivor buffer."""
+        survivors = []
+        ostart = 0
+        while ostart < self.R_outer:
+            ocount = min(self.ochunk, self.R_outer - ostart)
+            self.out_n.fill(0)
+            self._launch(ostart, ocount)
+            n = int(self.out_n.get()[0])
+            if n > self.out_cap:
+                raise RuntimeError(f"survivor buffer overflow ({n} > {self.out_cap}); raise max_survivors")
+            if n:
+                survivors.extend(int(x) for x in self.out[:n].get())
+            ostart += ocount
+        return survivors
+
+    def _verdict(self, t: int, surv: list[int], t0: float):
+        P = self.plan
+        cands = sorted(P.idx_to_n(i, t) for i in surv)
+        good = [n for n in cands if is_admissible(n, P.k)]
+        bad = [n for n in cands if n > P.k + 1 and n not in good]
+        return cands, good, bad
+
+    def search(self, max_blocks: int | None = None, log=None) -> dict:
+        """Blocks t = 0, 1, ... until the first block holding a good survivor.
+
+        Blocks are issued to the device several at a time as one block-ordered group: once a
+        good survivor is found in block t the kernel skips the group's later blocks, and the
+        device min-reduction names the block; every block up to it is scanned in full.  The
+        host then re-reads that block's survivors and re-verifies all of them."""
+        P = self.plan
+        t0 = time.time()
+        t = 0
+        # blocks per launch: grows geometrically (most searches end in the first few blocks),
+        # bounded by a position budget and by SEARCH_MAX_BLOCKS items per launch
+        cap = max(1, min(SEARCH_MAX_BLOCKS, (1 << int(P.tun.get("search_batch_log2", 34))) // max(P.R, 1)))
+        per = 1
+        while max_blocks is None or t < max_blocks:
+            nb = per if max_blocks is None else max(1, min(per, max_blocks - t))
+            per = min(cap, per * 4)
+            if nb == 1:
+                surv = self.scan_block(t)
+                found_t = t
+            else:
+                found = self._scan_blocks(t, nb)
+                if found is None:
+                    self.residues_checked += nb * P.R
+                    t += nb
+                    continue
+                found_t = found
+                self.residues_checked += (found_t - t) * P.R
+                surv = self.scan_block(found_t)
+            cands, good, bad = self._verdict(found_t, surv, t0)
+            if bad:
+                return {"k": P.k, "status": "DISAGREEMENT", "kernel_survivors": cands[:20],
+                        "ref_rejected": bad[:20], "block": found_t, "wall": time.time() - t0}
+            if log and (good or time.time() - getattr(self, "_last_log", 0) > 10):
+                self._last_log = time.time()
+                log(f"k={P.k} block t={found_t} survivors={len(surv)} good={len(good)} "
+                    f"checked={self.residues_checked:.3e} wall={time.time()-t0:.1f}s")
+            if good:
+                return {"k": P.k, "status": "FOUND", "g": good[0], "block": found_t,
+                        "survivors_in_block": len(surv), "residues_checked": self.residues_checked,
+                        "launches": self.launches, "wall": time.time() - t0}
+            t = found_t + 1
+        return {"k": P.k, "status": "EXHAUSTED_BLOCKS", "blocks": t,
+                "residues_checked": self.residues_checked, "wall": time.time() - t0}
+
+    def _scan_blocks(self, t: int, nb: int) -> int | None:
+        """One persistent launch over blocks [t, t+nb) as a block-ordered group; returns the
+        first block with a good survivor (device min-reduction) or None."""
+        items = [(0, 0, t + i, 0, self.R_outer) for i in range(nb)]
+        batch = N.Batch([self.ctx], items, self.tune)
+        try:
+            batch.run(use_graph=False)
+            self.launches += 1
+            m = batch.group_min(0)
+        finally:
+            batch.close()
+        return None if m is None else int(m[0])
+
+
+def free_vram_mib() -> int | None:
+    try:
+        o = subprocess.run(["nvidia-smi", "--query-gpu=memory.free", "--format=csv,noheader,nounits"],
+                           capture_output=True, text=True, timeout=10).stdout.strip().splitlines()[0]
+        return int(o)
+    except Exception:
+        return None
+
+
+def load_known(*paths: str) -> dict[int, tuple[int, str]]:
+    """k -> (g, source) from whitespace 'k g' files; earlier files win (sieve/gpu_sieve_v9.py:571-581)."""
+    known: dict[int, tuple[int, str]] = {}
+    for path in paths:
+        if not path or not os.path.exists(path):
+            continue
+        for line in open(path):
+            parts = line.split()
+            if len(parts) >= 2 and parts[0].isdigit() and parts[1].isdigit():
+                known.setdefault(int(parts[0]), (int(parts[1]), os.path.basename(path)))
+    return known
+
+
+def main():
+    """CLI/JSON contract of sieve/gpu_sieve_v9.py:584-618."""
+    ap = argparse.ArgumentParser(description="GB300 CRT-wheel search for g(k), partial-power wheel")
+    ap.add_argument("k", type=int, nargs="+")
+    ap.add_argument("--plan-only", action="store_true")
+    ap.add_argument("--tune", type=json.loads, default=None, help="JSON dict overriding TUNABLES")
+    ap.add_argument("--wheel", type=json.loads, default=None,
+                    help="explicit wheel: JSON list of [p,T] (or bare p = full power)")
+    ap.add_argument("--max-blocks", type=int, default=None)
+    ap.add_argument("--timeout", type=float, default=None, help="seconds; process exits 124 on expiry")
+    ap.add_argument("--min-free-mib", type=int, default=2048)
+    ap.add_argument("--bfile", default=os.path.join(HERE, "..", "data", "b003458.txt"))
+    ap.add_argument("--known", default=os.path.join(HERE, "..", "data", "known_extra.txt"))
+    a = ap.parse_args()
+    if a.timeout:
+        signal.signal(signal.SIGALRM, lambda *_: (print(json.dumps({"status": "TIMEOUT"}), flush=True), os._exit(124)))
+        signal.setitimer(signal.ITIMER_REAL, a.timeout)
+    known = load_known(a.bfile, a.known)
+    for k in a.k:
+        plan = Plan(k, a.tune, a.wheel)
+        if a.plan_only:
+            print(json.dumps(plan.summary()))
+            continue
+        free = free_vram_mib()
+        if free is not None and free < a.min_free_mib:
+            print(json.dumps({"k": k, "status": "SKIPPED_LOW_VRAM", "free_mib": free}))
+            continue
+        sieve = GpuSieve(plan)
+        res = sieve.search(a.max_blocks, log=lambda s: print(s, file=sys.stderr, flush=True))
+        if res.get("status") == "FOUND" and k in known:
+            g_known, src = known[k]
+            res["matches_bfile"] = (res["g"] == g_known)
+            res["bfile"] = g_known
+            res["known_source"] = src
+        res["plan"] = plan.summary()
+        print(json.dumps(res, default=str), flush=True)
+
+
+if __name__ == "__main__":
+    main()

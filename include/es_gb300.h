@@ -1,0 +1,178 @@
+/*
+ * es_gb300.h -- C ABI of the GB300 (sm_103a) Erdős–Selfridge CRT-wheel sieve engine.
+ *
+ * The library (libes_gb300.so) replaces the device half of the reference engine's
+ * GpuSieve object (sieve/gpu_sieve_v9.py:425-568, sieve/gpu_sieve_v11.py, and the word-mask
+ * variant sieve/es_word_masks.py:95-162).  The Python host (es_gb300.py) keeps the
+ * reference's Plan/GpuSieve surface and binds these entry points with ctypes.
+ *
+ * Conventions
+ *   - Every call returns int: ES_OK (0) or a negative ES_ERR_* code; es_last_error() gives a
+ *     one-line message for the calling thread.  Nothing throws across the ABI.
+ *   - Buffers passed in are caller-owned and copied before the call returns; contexts and
+ *     batches own all of their device memory.
+ *   - Launch calls are asynchronous on the context's own CUDA stream; the calls that return
+ *     results synchronise that stream first.  One host thread per context.
+ *   - Positions are block-relative indices idx = oidx * r0 + d0 in the ORIGINAL inner-ring
+ *     order (the reference's out[] contents, sieve/gpu_sieve_v9.py:325,
+ *     sieve/es_word_masks.py:44,88).  An "outer index" oidx covers one whole inner ring.
+ */
+#ifndef ES_GB300_H
+#define ES_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ES_ABI_VERSION 1
+
+#define ES_OK 0
+#define ES_ERR_ARG (-1)       /* bad argument or descriptor */
+#define ES_ERR_CUDA (-2)      /* CUDA runtime error (message in es_last_error) */
+#define ES_ERR_OVERFLOW (-3)  /* survivor buffer overflow: count exceeded capacity */
+#define ES_ERR_RANGE (-4)     /* outer range outside [0, R/r0) or size limit exceeded */
+#define ES_ERR_NOMEM (-5)     /* device or host allocation failed */
+#define ES_ERR_STATE (-6)     /* call out of order (e.g. results before a launch) */
+#define ES_ERR_NODEV (-7)     /* no CUDA device / device is not sm_103 */
+
+#define ES_LAYOUT_WORDMASK 0  /* phase word-mask tables: 32 candidates per load */
+#define ES_LAYOUT_SCALAR 1    /* per-candidate incremental residue + bit-table test */
+
+#define ES_MAX_MASK_FILTERS 8 /* filters evaluated in the inner-ring stage */
+#define ES_MAX_Q (1u << 20)   /* filter moduli q = p^t_p must be below 2^20 (k <= 1024) */
+
+typedef struct es_ctx es_ctx;
+typedef struct es_batch es_batch;
+
+/* One wheel plan (the reference's Plan, sieve/gpu_sieve_v9.py:344-383), flattened.
+ * Rings are in the plan's ring order (ring 0 = inner ring swept per outer index, ring 1 the
+ * next-fastest digit, ...); the terms of ring j are (residue * basis_j) mod M for every
+ * admissible residue of the ring, in the ring's sorted residue order -- exactly the
+ * reference's term_lo/term_hi arrays (sieve/gpu_sieve_v9.py:433-437).  Filters are the
+ * residual primes in cascade order with their full-power modulus q = p^t_p and a packed
+ * bit table of admissible residues, ceil(q/32) little-endian words each, concatenated
+ * (sieve/gpu_sieve_v11.py bit-packed tables). */
+typedef struct es_plan_desc {
+    uint32_t k;
+    uint32_t n_rings;          /* may be 0 (no wheel: M = 1) */
+    uint32_t n_filters;
+    uint32_t flags;            /* reserved, must be 0 */
+    uint64_t M_lo, M_hi;       /* wheel modulus, 1 <= M < 2^126 */
+    const uint32_t* radix;     /* [n_rings] admissible residues per ring */
+    const uint64_t* term_lo;   /* [sum radix] low 64 bits of the ring terms */
+    const uint64_t* term_hi;   /* [sum radix] high 64 bits */
+    const uint32_t* filter_q;  /* [n_filters] moduli, each < ES_MAX_Q */
+    const uint32_t* allowed;   /* [sum ceil(q/32)] packed admissible-residue bits */
+} es_plan_desc;
+
+/* Launch shape and table layout; chosen by the autotuner (es_autotune.py).  None of these
+ * changes which candidates pass. */
+typedef struct es_tune {
+    uint32_t layout;        /* ES_LAYOUT_WORDMASK or ES_LAYOUT_SCALAR */
+    uint32_t mask_filters;  /* filters in the inner-ring stage, 1..ES_MAX_MASK_FILTERS */
+    uint32_t threads;       /* CTA size, multiple of 32 in [64, 512] */
+    uint32_t strip;         /* ring-1 cycles per thread per work unit (strip depth) */
+    uint32_t smem_kb;       /* shared-memory budget per CTA for staged tables */
+    uint32_t ctas_per_sm;   /* persistent grid = SM count * ctas_per_sm */
+    uint32_t count_stages;  /* 1: accumulate per-filter-stage pass counts */
+    uint32_t reserved;
+} es_tune;
+
+/* One survivor of the full cascade (kernel emit, sieve/gpu_sieve_v9.py:323-326). */
+typedef struct es_survivor {
+    uint64_t idx;       /* block-relative position index, original inner order */
+    uint64_t s_lo;      /* n mod M, low 64 bits */
+    uint64_t s_hi;      /* n mod M, high 64 bits */
+    uint64_t t;         /* block: n = t*M + s */
+    uint32_t item;      /* batch item that produced it (0 for es_launch) */
+    uint32_t good;      /* 1 iff n > k + 1 */
+} es_survivor;
+
+/* One work item of a persistent batch launch: a block t of one plan and an outer-index range.
+ * Items sharing a group form one block-ordered search: a good survivor in block t lets the
+ * kernel skip the group's later blocks (t' > t), never blocks <= t. */
+typedef struct es_batch_item {
+    uint32_t ctx_index;   /* index into the ctx array given to es_batch_create */
+    uint32_t group;       /* search group id, < n_items */
+    uint64_t t;           /* block index */
+    uint64_t o_begin;     /* outer-index range [o_begin, o_end) within [0, R/r0) */
+    uint64_t o_end;
+} es_batch_item;
+
+/* ---- library ------------------------------------------------------------------------- */
+const char* es_last_error(void);
+int es_abi_version(void);
+/* Device facts for the tuner: SM count, compute capability, opt-in shared memory per CTA. */
+int es_device_info(int* sm_count, int* cc_major, int* cc_minor, uint64_t* smem_optin_bytes);
+
+/* ---- context: one plan on the device ---------------------------------------------------- */
+/* Replaces GpuSieve.__init__ (sieve/gpu_sieve_v9.py:426-498): copies term tables, filter bit
+ * tables, and builds every derived table (sorted inner ring, carry-split keys, ring-1/ring-2
+ * residue tables, word-mask phase tables) on the host in C++, then uploads them once. */
+int es_ctx_create(const es_plan_desc* desc, const es_tune* tune, es_ctx** out);
+/* Releases the context's device memory (the reference relied on CuPy garbage collection). */
+int es_ctx_destroy(es_ctx* ctx);
+int es_ctx_set_tune(es_ctx* ctx, const es_tune* tune);
+int es_ctx_get_tune(const es_ctx* ctx, es_tune* tune);
+/* Geometry: R/r0 outer indices, inner radix r0, filter count, bytes of derived tables. */
+int es_ctx_info(const es_ctx* ctx, uint64_t* n_outer, uint32_t* r0, uint32_t* n_filters,
+                uint64_t* table_bytes);
+/* Survivor capacity (reference TUNABLES max_survivors, sieve/gpu_sieve_v9.py:107). */
+int es_set_capacity(es_ctx* ctx, uint64_t cap);
+
+/* Per-block constants tconst[j] = (t mod q_j)(M mod q_j) mod q_j for every filter; replaces
+ * sieve.tconst.set(tconst_h) (harness/run_k.py:102-104, sieve/gpu_sieve_v9.py:512-514). */
+int es_set_block(es_ctx* ctx, const uint32_t* tconst, uint32_t n_filters, uint64_t t);
+/* Replaces out_n.fill(0) (harness/run_k.py:118, sieve/gpu_sieve_v9.py:515). */
+int es_reset_survivors(es_ctx* ctx);
+/* Replaces GpuSieve._launch(ostart, ocount) (sieve/gpu_sieve_v9.py:500-506): scans outer
+ * indices [ostart, ostart+ocount) of the current block; asynchronous; survivors accumulate
+ * until es_reset_survivors. */
+int es_launch(es_ctx* ctx, uint64_t ostart, uint64_t ocount);
+/* Same scan over an explicit list of outer indices (seeded sub-samples). */
+int es_launch_list(es_ctx* ctx, const uint64_t* outer, uint64_t n);
+int es_sync(es_ctx* ctx);
+/* Replaces int(out_n.get()[0]) (harness/run_k.py:120): synchronises, returns the count of
+ * survivors since the last reset (may exceed capacity: then ES_ERR_OVERFLOW on read). */
+int es_survivor_count(es_ctx* ctx, uint64_t* n);
+/* Replaces out[:n].get() (harness/run_k.py:124): block-relative indices, device order. */
+int es_read_survivors(es_ctx* ctx, uint64_t* idx_out, uint64_t cap, uint64_t* n);
+int es_read_survivor_records(es_ctx* ctx, es_survivor* out, uint64_t cap, uint64_t* n);
+/* Per-filter-stage pass counts since the last es_reset_counts: counts[j] = positions whose
+ * n passed filters 0..j of the cascade (order-dependent).  No reference counterpart beyond
+ * the docstring estimates (sieve/gpu_sieve_v9.py:1-27); needs tune.count_stages = 1. */
+int es_stage_counts(es_ctx* ctx, uint64_t* counts, uint32_t n_filters);
+int es_reset_counts(es_ctx* ctx);
+/* Block-ordered minimum over the survivors since the last reset: the least n = t*M + s with
+ * n > k+1 (replaces the host sort + first good in GpuSieve.search, gpu_sieve_v9.py:551-563;
+ * the host still re-verifies it). found = 0 when there is none. */
+int es_min_survivor(es_ctx* ctx, int* found, uint64_t* t, uint64_t* s_lo, uint64_t* s_hi);
+/* Launch + CUDA-event time of the scan kernel alone (milliseconds), synchronising. */
+int es_launch_timed(es_ctx* ctx, uint64_t ostart, uint64_t ocount, float* ms);
+
+/* ---- persistent batch: many (plan, block, range) scans in one work-stealing launch ------- */
+int es_batch_create(es_ctx* const* ctxs, uint32_t n_ctx, const es_batch_item* items,
+                    uint32_t n_items, const es_tune* tune, es_batch** out);
+/* Resets counters and survivors, then runs the persistent scan kernel and the block-ordered
+ * min-reduction; use_graph = 1 replays a captured CUDA graph of that sequence. */
+int es_batch_run(es_batch* b, int use_graph);
+/* Synchronises; ms = device time of the last run (CUDA events around the whole sequence). */
+int es_batch_sync(es_batch* b, float* ms);
+int es_batch_group_min(es_batch* b, uint32_t group, int* found, uint64_t* t, uint64_t* s_lo,
+                       uint64_t* s_hi);
+int es_batch_item_counts(es_batch* b, uint32_t item, uint64_t* counts, uint32_t n_filters);
+int es_batch_survivors(es_batch* b, es_survivor* out, uint64_t cap, uint64_t* n);
+/* Units claimed per item in the last run (units of skipped blocks included), for tests. */
+int es_batch_destroy(es_batch* b);
+
+/* ---- measurement -------------------------------------------------------------------------- */
+/* Integer-pipe peak microbenchmark: int32 operations per second of a dependent-free mix of
+ * IADD3 / LOP3 / IMAD-class instructions across the whole GPU (ops = lanes x instructions). */
+int es_int_peak(double* ops_per_s, double* ms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ES_GB300_H */
