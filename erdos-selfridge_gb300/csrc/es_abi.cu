@@ -80,8 +80,8 @@ int check_tune(const es_tune& t) {
         return fail(ES_ERR_ARG, "tune.layout must be 0 (word-mask) or 1 (scalar)");
     if (t.mask_filters < 1 || t.mask_filters > ES_MAX_MASK_FILTERS)
         return fail(ES_ERR_ARG, "tune.mask_filters must be in 1..8");
-    if (t.threads < 64 || t.threads > 512 || t.threads % 32)
-        return fail(ES_ERR_ARG, "tune.threads must be a multiple of 32 in [64, 512]");
+    if (t.threads < 64 || t.threads > 1024 || t.threads % 32)
+        return fail(ES_ERR_ARG, "tune.threads must be a multiple of 32 in [64, 1024]");
     if (t.strip < 1 || t.strip > 4096) return fail(ES_ERR_ARG, "tune.strip must be in 1..4096");
     if (t.ctas_per_sm < 1 || t.ctas_per_sm > 16)
         return fail(ES_ERR_ARG, "tune.ctas_per_sm must be in 1..16");
@@ -156,6 +156,7 @@ struct es_batch {
     unsigned long long* d_min = nullptr;
     EsLaunch L{};
     int grid = 0;
+    uint32_t words = 0;  // inner-ring words shared by every plan, 0 when they differ
     bool ran = false;
 };
 
@@ -163,13 +164,19 @@ namespace {
 
 // Shared-memory plan of one launch: [small | fast tables | tconst | counters].
 struct SmemPlan {
-    uint32_t fast_off, tconst_off, cnt_off, bytes;
+    uint32_t fast_off, tconst_off, cnt_off, queue_off, bytes;
     uint32_t fast_words_cap;
 };
 
+// per-warp survivor queue (64 entries x 24 bytes), must match the kernel's EsQueue
+constexpr uint32_t kQueueBytes = 64u * 24u;
+
 SmemPlan plan_smem(uint32_t small_max, uint32_t nf_max, const es_tune& tune, uint32_t fast_need) {
     SmemPlan p;
-    const uint32_t fixed_tail = (uint32_t)align_up(4u * nf_max, 16) * 2u;
+    const uint32_t warps = tune.threads / 32u;
+    const uint32_t queues = kQueueBytes * warps;
+    const uint32_t counters = (uint32_t)align_up(4ull * nf_max * warps, 16);
+    const uint32_t fixed_tail = counters + queues;
     uint32_t budget = tune.smem_kb * 1024u;
     const uint32_t optin = (uint32_t)(g_dev.smem_optin - 1024);
     if (budget > optin) budget = optin;
@@ -179,8 +186,9 @@ SmemPlan plan_smem(uint32_t small_max, uint32_t nf_max, const es_tune& tune, uin
     p.fast_off = small_max;
     p.fast_words_cap = fast_bytes / 4u;
     p.tconst_off = p.fast_off + fast_bytes;
-    p.cnt_off = p.tconst_off + (uint32_t)align_up(4u * nf_max, 16);
-    p.bytes = p.cnt_off + (uint32_t)align_up(4u * nf_max, 16);
+    p.cnt_off = p.tconst_off;
+    p.queue_off = p.cnt_off + counters;
+    p.bytes = p.queue_off + queues;
     return p;
 }
 
@@ -202,10 +210,10 @@ uint32_t fast_need(const es_ctx* c, uint32_t layout, uint32_t F) {
     return pre[std::min<uint32_t>(F, (uint32_t)pre.size() - 1)];
 }
 
-int grid_for(uint32_t layout, uint32_t count, const es_tune& tune, uint32_t smem, uint64_t units,
-             int* grid) {
+int grid_for(uint32_t layout, uint32_t count, uint32_t words, const es_tune& tune, uint32_t smem,
+             uint64_t units, int* grid) {
     int occ = 0;
-    int e = es_scan_occupancy((int)layout, (int)count, tune.mask_filters, (int)tune.threads,
+    int e = es_scan_occupancy((int)layout, (int)count, words, tune.mask_filters, (int)tune.threads,
                               (int)smem, &occ);
     if (e) return cuda_fail((cudaError_t)e, "occupancy");
     if (occ < 1) return fail(ES_ERR_ARG, "launch shape does not fit one SM (threads/smem)");
@@ -366,8 +374,8 @@ int es_ctx_create(const es_plan_desc* d, const es_tune* tune_in, es_ctx** out) {
     I.o_TQ1 = take(4ull * ES_FMAX * r1);
     I.o_D2 = take(16ull * r2);
     I.o_DQ2 = take(4ull * ES_FMAX * r2);
-    I.o_S0 = take(16ull * r0);
-    I.o_K0 = take(4ull * r0);
+    I.o_S0 = take(16ull * (r0 + 1));   // + sentinel S0[r0] = M
+    I.o_K0 = take(4ull * (r0 + 1));    // + sentinel K0[r0] = 0xffffffff
     I.o_I0 = take(4ull * r0);
     I.o_Q0 = take(4ull * ES_FMAX * r0);
     I.o_BK = take(2ull * (ES_NBUCKET + 1));
@@ -397,6 +405,8 @@ int es_ctx_create(const es_plan_desc* d, const es_tune* tune_in, es_ctx** out) {
         put32(I.o_I0, i, order[i]);
         for (uint32_t f = 0; f < FB; ++f) put32(I.o_Q0, f * r0 + i, mod_q(S0[i], c->q[f]));
     }
+    put128(I.o_S0, r0, M);             // stops the tie scan: M < thr never holds (thr <= M)
+    put32(I.o_K0, r0, 0xffffffffu);    // stops the key scan: never < t32
     memcpy(&small[I.o_BK], BK.data(), 2ull * (ES_NBUCKET + 1));
     if (nf) memcpy(&small[I.o_FC], fc.data(), sizeof(EsFilterC) * nf);
 
@@ -571,7 +581,7 @@ static int ctx_launch(es_ctx* c, uint64_t ob, uint64_t oe, const uint64_t* d_lis
         n_work = cycles_of(I, ob, oe, &it.c_begin);
         it.c_end = it.c_begin + n_work;
     }
-    const uint64_t per_unit = (uint64_t)tn.threads * tn.strip;
+    const uint64_t per_unit = 32ull * tn.strip;
     it.unit_begin = 0;
     it.n_units = (n_work + per_unit - 1) / per_unit;
     it.group = 0;
@@ -585,7 +595,9 @@ static int ctx_launch(es_ctx* c, uint64_t ob, uint64_t oe, const uint64_t* d_lis
     L.strip = tn.strip;
     L.mask_filters = tn.mask_filters;
     L.total_units = it.n_units;
-    L.cycles_per_unit = per_unit;
+    L.chunk_max = 16u * (tn.threads / 32u);
+    L.nf_max = std::max<uint32_t>(I.n_filters, 1);
+    L.direct = 1;
     L.unit_counter = c->d_unit;
     L.surv = c->d_surv;
     L.surv_n = c->d_surv_n;
@@ -595,12 +607,13 @@ static int ctx_launch(es_ctx* c, uint64_t ob, uint64_t oe, const uint64_t* d_lis
     L.tconst_off = sp.tconst_off;
     L.fast_off = sp.fast_off;
     L.cnt_off = sp.cnt_off;
+    L.queue_off = sp.queue_off;
     memcpy(L.tconst0, c->tconst, 4ull * I.n_filters);
     if (it.n_units == 0) return ES_OK;
     int grid = 0;
-    if (int e = grid_for(tn.layout, tn.count_stages, tn, sp.bytes, it.n_units, &grid)) return e;
+    if (int e = grid_for(tn.layout, tn.count_stages, I.W, tn, sp.bytes, it.n_units, &grid)) return e;
     ES_CUDA(cudaMemsetAsync(c->d_unit, 0, 8, c->stream), "memset");
-    int e = es_launch_scan(L, (int)tn.layout, (int)tn.count_stages, grid, c->stream);
+    int e = es_launch_scan(L, (int)tn.layout, (int)tn.count_stages, I.W, grid, c->stream);
     if (e) return cuda_fail((cudaError_t)e, "scan launch");
     c->launched = true;
     return ES_OK;
@@ -746,7 +759,10 @@ int es_batch_create(es_ctx* const* ctxs, uint32_t n_ctx, const es_batch_item* it
         need_max = std::max<uint32_t>(need_max, fast_need(c, tune.layout, F));
     }
     const SmemPlan sp = plan_smem(small_max, nf_max, tune, need_max);
-    const uint64_t per_unit = (uint64_t)tune.threads * tune.strip;
+    const uint64_t per_unit = 32ull * tune.strip;
+    b->words = ctxs[0]->h_inst.W;
+    for (uint32_t i = 1; i < n_ctx; ++i)
+        if (ctxs[i]->h_inst.W != b->words) b->words = 0;
     std::vector<uint32_t> h_tc;
     b->h_items.resize(n_items);
     b->count_off.resize(n_items);
@@ -824,7 +840,9 @@ int es_batch_create(es_ctx* const* ctxs, uint32_t n_ctx, const es_batch_item* it
     L.strip = tune.strip;
     L.mask_filters = tune.mask_filters;
     L.total_units = units;
-    L.cycles_per_unit = per_unit;
+    L.chunk_max = 16u * (tune.threads / 32u);
+    L.nf_max = nf_max;
+    L.direct = n_ctx == 1 ? 1u : 0u;
     L.unit_counter = b->d_unit;
     L.surv = b->d_surv;
     L.surv_n = b->d_surv_n;
@@ -834,7 +852,8 @@ int es_batch_create(es_ctx* const* ctxs, uint32_t n_ctx, const es_batch_item* it
     L.tconst_off = sp.tconst_off;
     L.fast_off = sp.fast_off;
     L.cnt_off = sp.cnt_off;
-    if (int e = grid_for(tune.layout, tune.count_stages, tune, sp.bytes, std::max<uint64_t>(units, 1), &b->grid)) {
+    L.queue_off = sp.queue_off;
+    if (int e = grid_for(tune.layout, tune.count_stages, b->words, tune, sp.bytes, std::max<uint64_t>(units, 1), &b->grid)) {
         es_batch_destroy(b);
         return e;
     }
@@ -848,7 +867,7 @@ static int batch_enqueue(es_batch* b) {
     if (b->counts_words)
         ES_CUDA(cudaMemsetAsync(b->d_counts, 0, 8ull * b->counts_words, b->stream), "memset");
     if (b->L.total_units) {
-        int e = es_launch_scan(b->L, (int)b->tune.layout, (int)b->tune.count_stages, b->grid, b->stream);
+        int e = es_launch_scan(b->L, (int)b->tune.layout, (int)b->tune.count_stages, b->words, b->grid, b->stream);
         if (e) return cuda_fail((cudaError_t)e, "scan launch");
     }
     int e = es_launch_min(b->d_surv, b->d_surv_n, b->surv_cap, b->d_items, b->n_groups, b->d_min, b->stream);

@@ -83,18 +83,21 @@ struct EsLaunch {
     uint32_t threads;
     uint32_t strip;
     uint32_t mask_filters;   // F requested (template F is the rounded-up instance)
-    uint64_t total_units;
-    uint64_t cycles_per_unit;      // threads * strip
+    uint64_t total_units;          // warp-units: 32 lanes x strip ring-1 cycles (or list entries)
+    uint32_t chunk_max;            // most warp-units a CTA claims at once
+    uint32_t nf_max;               // largest filter count among the launch's plans
+    uint32_t direct;               // 1: every item uses one plan (no CTA barriers after staging)
+    uint32_t pad2;
     unsigned long long* unit_counter;
     struct es_survivor* surv;
     unsigned long long* surv_n;
     uint64_t surv_cap;
     unsigned long long* group_found;  // per group: least block with a good survivor
     uint32_t smem_bytes;              // dynamic shared memory of the launch
-    uint32_t tconst_off;              // byte offset of the staged tconst in smem
+    uint32_t tconst_off;              // unused (block constants are read from the item)
     uint32_t fast_off;                // byte offset of the staged fast tables in smem
-    uint32_t cnt_off;                 // byte offset of the per-stage counters in smem
-    uint32_t pad1;
+    uint32_t cnt_off;                 // byte offset of the per-warp tail-stage counters in smem
+    uint32_t queue_off;               // byte offset of the per-warp survivor queues in smem
     // single-plan launches carry their one item and block constants by value
     EsItem item0;
     uint32_t tconst0[ES_MAX_FILTERS];
@@ -102,9 +105,10 @@ struct EsLaunch {
 
 // Host-side launchers implemented in es_scan.cu (return a cudaError_t value).
 int es_scan_prepare(int smem_optin_bytes);
-int es_scan_occupancy(int layout, int count, uint32_t mask_filters, int threads, int smem_bytes,
-                      int* ctas_per_sm);
-int es_launch_scan(const EsLaunch& L, int layout, int count, int grid, void* stream);
+// words: inner-ring words per outer index (1, 2, or anything else for the generic instance)
+int es_scan_occupancy(int layout, int count, uint32_t words, uint32_t mask_filters, int threads,
+                      int smem_bytes, int* ctas_per_sm);
+int es_launch_scan(const EsLaunch& L, int layout, int count, uint32_t words, int grid, void* stream);
 // group_min: [n_groups][4] = {found, t, s_lo, s_hi}; items == nullptr means one group (0)
 int es_launch_min(const struct es_survivor* surv, const unsigned long long* surv_n,
                   uint64_t cap, const EsItem* items, uint32_t n_groups,

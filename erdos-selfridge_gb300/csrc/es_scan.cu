@@ -9,65 +9,106 @@
 // accumulated on request.  All arithmetic is exact integer arithmetic.
 //
 // How it is organised (GB300-first, not the reference's per-plan NVRTC source):
-//  * One persistent kernel per launch; CTAs claim work units (threads x strip ring-1 cycles
-//    of one item) from a global atomic counter -- no spin waits anywhere.  Items are ordered
-//    by (group, block), and a group's later blocks are skipped once a good survivor is known.
-//  * Two-level strip mining.  A thread owns `strip` consecutive ring-1 cycles (cycle index =
+//  * One persistent kernel per launch; warps claim work units from a global atomic counter --
+//    no spin waits anywhere.  Items are ordered by (group, block), and a group's later blocks
+//    are skipped once a good survivor is known (block-ordered search).
+//  * Two-level strip mining.  A lane owns `strip` consecutive ring-1 cycles (cycle index =
 //    oidx / r1).  Rings >= 2 give b2 = sum term_j mod M, decoded once per strip and then
 //    stepped with a 128-bit delta table when the ring-2 digit advances.  Ring 1 is swept in a
-//    warp-uniform loop (b = b2 + T1[d1], broadcast loads), and ring 0 (the inner ring) is
+//    warp-uniform loop (b = b2 + T1[d1], broadcast loads) and ring 0, the inner ring, is
 //    handled 32 candidates at a time as bit masks.
-//  * Filter residues are carried incrementally in 32-bit arithmetic: BQ_f = n mod q_f for the
-//    ring-0 base, updated with precomputed term residues and the wrap correction
-//    corr_f = -M mod q_f (the reference's v7 identity, sieve/gpu_sieve_v9.py:9-18).
-//  * Inner ring: the terms are sorted once on the host, so the wrap (s >= M) is a suffix of
-//    the sorted slots; its start (the carry split) is found from 32-bit keys via a 1024-bucket
-//    table.  Word-mask layout: a filter is one or two table loads per 32 candidates,
+//  * 128-bit values are four 32-bit limbs with PTX carry chains; filter residues are carried
+//    incrementally in 32-bit arithmetic: BQ_f = n mod q_f for the ring-0 base, updated from
+//    precomputed term residues and the wrap correction corr_f = -M mod q_f (the reference's v7
+//    identity, sieve/gpu_sieve_v9.py:9-18), reduced with unsigned min instead of branches.
+//  * Inner ring: its terms are sorted once on the host, so the wrap (s >= M) is a suffix of the
+//    sorted slots; its start (the carry split) comes from 32-bit keys through a 1024-bucket
+//    table.  Word-mask layout: a filter costs two table loads per 32 candidates,
 //    P_f[phase][w]; scalar layout: one residue + bit test per live candidate.  A warp leaves
-//    the cascade early as soon as a ballot shows no live candidate.
-//  * Filters after the inner-ring stage are evaluated per surviving candidate from the exact
-//    128-bit residue with limb weights and a Barrett reduction.
+//    the cascade early when a ballot shows no live candidate.
+//  * Candidates passing the inner-ring stage are queued per warp and run through the exact
+//    remaining filters 32 at a time (full warps, not single lanes), from the 128-bit residue
+//    with limb weights and a Barrett reduction.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
 #include "../../include/es_gb300.h"
 #include "es_internal.h"
 
-typedef unsigned __int128 u128;
-
 namespace {
 
-__device__ __forceinline__ u128 mk128(uint64_t lo, uint64_t hi) {
-    return ((u128)hi << 64) | (u128)lo;
+// 128-bit value as little-endian 32-bit limbs.
+struct U4 {
+    uint32_t x, y, z, w;
+};
+
+__device__ __forceinline__ U4 u4(const uint4 v) { return U4{v.x, v.y, v.z, v.w}; }
+
+__device__ __forceinline__ U4 add128(const U4 a, const U4 b) {
+    U4 r;
+    asm("add.cc.u32 %0, %4, %8;\n\t"
+        "addc.cc.u32 %1, %5, %9;\n\t"
+        "addc.cc.u32 %2, %6, %10;\n\t"
+        "addc.u32 %3, %7, %11;"
+        : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w)
+        : "r"(a.x), "r"(a.y), "r"(a.z), "r"(a.w), "r"(b.x), "r"(b.y), "r"(b.z), "r"(b.w));
+    return r;
 }
 
-// (a + b) mod M for a, b < M < 2^126; wrap = 1 when M was subtracted.
-__device__ __forceinline__ u128 addmod(u128 a, u128 b, u128 M, uint32_t& wrap) {
-    u128 s = a + b;
-    wrap = (s >= M) ? 1u : 0u;
-    return wrap ? s - M : s;
+// r = a - b; borrow = 0xffffffff when a < b, else 0.
+__device__ __forceinline__ U4 sub128(const U4 a, const U4 b, uint32_t& borrow) {
+    U4 r;
+    asm("sub.cc.u32 %0, %5, %9;\n\t"
+        "subc.cc.u32 %1, %6, %10;\n\t"
+        "subc.cc.u32 %2, %7, %11;\n\t"
+        "subc.cc.u32 %3, %8, %12;\n\t"
+        "subc.u32 %4, 0, 0;"
+        : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w), "=r"(borrow)
+        : "r"(a.x), "r"(a.y), "r"(a.z), "r"(a.w), "r"(b.x), "r"(b.y), "r"(b.z), "r"(b.w));
+    return r;
 }
 
-// x mod q for a 128-bit x, q < 2^20: limb weights then one Barrett step.
-__device__ __forceinline__ uint32_t mod128(u128 x, const EsFilterC& f) {
-    const uint64_t lo = (uint64_t)x, hi = (uint64_t)(x >> 64);
-    const uint64_t y = (lo & 0xffffffffull) + (lo >> 32) * f.w1 + (hi & 0xffffffffull) * f.w2 +
-                       (hi >> 32) * f.w3;
+__device__ __forceinline__ U4 sel128(uint32_t mask, const U4 a, const U4 b) {  // mask ? a : b
+    return U4{(a.x & mask) | (b.x & ~mask), (a.y & mask) | (b.y & ~mask), (a.z & mask) | (b.z & ~mask),
+              (a.w & mask) | (b.w & ~mask)};
+}
+
+// (a + b) mod M for a, b < M < 2^126; wmask = 0xffffffff when M was subtracted.
+__device__ __forceinline__ U4 addmod(const U4 a, const U4 b, const U4 M, uint32_t& wmask) {
+    const U4 s = add128(a, b);
+    uint32_t br;
+    const U4 d = sub128(s, M, br);
+    wmask = ~br;
+    return sel128(br, s, d);
+}
+
+__device__ __forceinline__ bool lt128(const U4 a, const U4 b) {
+    uint32_t br;
+    sub128(a, b, br);
+    return br != 0u;
+}
+
+__device__ __forceinline__ uint64_t lo64(const U4 a) { return ((uint64_t)a.y << 32) | a.x; }
+__device__ __forceinline__ uint64_t hi64(const U4 a) { return ((uint64_t)a.w << 32) | a.z; }
+
+// x mod q for a 128-bit x, q < 2^20: limb weights (2^32i mod q) then one Barrett step.
+__device__ __forceinline__ uint32_t mod128(const U4 x, const EsFilterC& f) {
+    const uint64_t y = (uint64_t)x.x + (uint64_t)x.y * f.w1 + (uint64_t)x.z * f.w2 + (uint64_t)x.w * f.w3;
     const uint64_t qt = __umul64hi(y, f.rcp);
     uint64_t r = y - qt * f.q;
     if (r >= f.q) r -= f.q;
     return (uint32_t)r;
 }
 
-__device__ __forceinline__ uint32_t red2(uint32_t v, uint32_t q) {
-    v = (v >= q) ? v - q : v;
-    return (v >= q) ? v - q : v;
-}
+// v mod q for v < 2q (unsigned min: v - q wraps to a huge value when v < q)
+__device__ __forceinline__ uint32_t red1(uint32_t v, uint32_t q) { return min(v, v - q); }
+// v mod q for v < 3q
+__device__ __forceinline__ uint32_t red2(uint32_t v, uint32_t q) { return red1(red1(v, q), q); }
 
 // b2 = sum_{j>=2} term_j[d_j] mod M for ring-1 cycle c; also returns the ring-2 digit.
-__device__ __noinline__ u128 decode_cycle(const EsInst& I, uint64_t c, u128 M, uint32_t& d2) {
+__device__ __noinline__ U4 decode_cycle(const EsInst& I, uint64_t c, const U4 M, uint32_t& d2) {
     uint64_t rem = c;
-    u128 acc = 0;
+    U4 acc{0u, 0u, 0u, 0u};
     d2 = 0;
     for (uint32_t j = 2; j < I.n_rings; ++j) {
         const uint32_t r = __ldg(I.radix + j);
@@ -81,9 +122,9 @@ __device__ __noinline__ u128 decode_cycle(const EsInst& I, uint64_t c, u128 M, u
             rem = rem / r;
         }
         if (j == 2) d2 = (uint32_t)d;
-        const uint64_t* tp = I.ring_terms + 2ull * ((uint64_t)__ldg(I.ring_off + j) + d);
-        uint32_t w;
-        acc = addmod(acc, mk128(__ldg(tp), __ldg(tp + 1)), M, w);
+        const uint4 tv = __ldg(reinterpret_cast<const uint4*>(I.ring_terms) + (__ldg(I.ring_off + j) + d));
+        uint32_t wm;
+        acc = addmod(acc, u4(tv), M, wm);
     }
     return acc;
 }
@@ -98,314 +139,479 @@ __device__ __forceinline__ void copy_words(uint32_t* dst, const uint32_t* __rest
     for (uint32_t i = (n4 << 2) + threadIdx.x; i < nwords; i += blockDim.x) dst[i] = __ldg(src + i);
 }
 
-struct EsSmemView {
-    const ulonglong2* T1;
-    const uint32_t* TQ1;
-    const ulonglong2* D2;
-    const uint32_t* DQ2;
-    const ulonglong2* S0;
-    const uint32_t* K0;
-    const uint32_t* I0;
-    const uint32_t* Q0;
-    const uint16_t* BK;
-    const EsFilterC* FC;
-    const uint32_t* tc;
-    const uint32_t* fast;
+// Per-warp queue of candidates that passed the inner-ring stage; the exact cascade tail runs
+// on 32 queued candidates at a time so that whole warps, not single lanes, do the 128-bit work.
+#define ES_QCAP 64
+struct EsQueue {
+    uint4 s[ES_QCAP];                  // n mod M, 32-bit limbs
+    unsigned long long idx[ES_QCAP];   // block-relative position index
 };
 
-template <bool COUNT>
-__device__ __forceinline__ void emit(const EsLaunch& L, const EsItem& item, const EsInst& I,
-                                     uint32_t item_id, uint64_t idx, u128 s, u128 M) {
-    const u128 kp1 = (u128)(I.k + 1u);
-    bool good;
-    if (M > kp1) {
-        good = (item.t > 0) || (s > kp1);
-    } else {
-        good = ((u128)item.t * M + s) > kp1;
-    }
-    const unsigned long long slot = atomicAdd(L.surv_n, 1ull);
-    if (slot < L.surv_cap) {
-        es_survivor* r = L.surv + slot;
-        r->idx = idx;
-        r->s_lo = (uint64_t)s;
-        r->s_hi = (uint64_t)(s >> 64);
-        r->t = item.t;
-        r->item = item_id;
-        r->good = good ? 1u : 0u;
-    }
-    if (good && L.group_found) atomicMin(L.group_found + item.group, (unsigned long long)item.t);
+__device__ __forceinline__ void red_add_shared(uint32_t saddr, uint32_t v) {
+    // Not visible to the compiler as a store: the counters are read only after a __syncwarp.
+    asm volatile("red.shared.add.u32 [%0], %1;" ::"r"(saddr), "r"(v));
 }
 
-// Exact cascade tail for one candidate: filters [f0, nf) from the 128-bit residue s.
+#ifndef ES_LB_THREADS
+#define ES_LB_THREADS 512   // largest CTA the scan kernel is compiled for
+#endif
+#ifndef ES_LB_MINB
+#define ES_LB_MINB 1
+#endif
+
+// Everything the cascade tail and the emit need for one item, passed by value into the
+// force-inlined helpers below (nothing escapes to local memory).
+struct TailCtx {
+    U4 M;
+    uint64_t M_lo;
+    uint64_t t_blk;
+    const EsFilterC* sFC;
+    const uint32_t* tc;
+    const uint32_t* allowed_g;
+    es_survivor* surv;
+    unsigned long long* surv_n;
+    unsigned long long* group_found;
+    uint64_t surv_cap;
+    uint32_t kp1, Feff, nf, wcnt_saddr, item_id, group;
+    bool M_big;
+};
+
+// exact tail of the cascade for one candidate (filters Feff..nf-1), then the emit
 template <bool COUNT>
-__device__ __forceinline__ bool tail_filters(const EsSmemView& V, const EsInst& I, uint32_t f0,
-                                             u128 s, uint32_t* sm_cnt) {
-    for (uint32_t f = f0; f < I.n_filters; ++f) {
-        const EsFilterC fc = V.FC[f];
-        uint32_t r = mod128(s, fc) + V.tc[f];
+__device__ __forceinline__ void tail_one(const TailCtx& C, const U4 s, uint64_t idx) {
+    for (uint32_t f = C.Feff; f < C.nf; ++f) {
+        const EsFilterC fc = C.sFC[f];
+        uint32_t r = mod128(s, fc) + C.tc[f];
         if (r >= fc.q) r -= fc.q;
-        const uint32_t w = __ldg(I.allowed + fc.off + (r >> 5));
-        if (!((w >> (r & 31u)) & 1u)) return false;
-        if (COUNT) atomicAdd(sm_cnt + f, 1u);
+        const uint32_t wv = __ldg(C.allowed_g + fc.off + (r >> 5));
+        if (!((wv >> (r & 31u)) & 1u)) return;
+        if (COUNT) red_add_shared(C.wcnt_saddr + 4u * f, 1u);
     }
-    return true;
+    bool good;
+    if (C.M_big) {
+        good = (C.t_blk > 0) || s.w || s.z || s.y || (s.x > C.kp1);
+    } else {
+        const uint64_t n = C.t_blk * C.M_lo + s.x;   // M <= k+1 <= 1025: n fits easily
+        good = n > C.kp1;
+    }
+    const unsigned long long slot = atomicAdd(C.surv_n, 1ull);
+    if (slot < C.surv_cap) {
+        es_survivor* rec = C.surv + slot;
+        rec->idx = idx;
+        rec->s_lo = lo64(s);
+        rec->s_hi = hi64(s);
+        rec->t = C.t_blk;
+        rec->item = C.item_id;
+        rec->good = good ? 1u : 0u;
+    }
+    if (good && C.group_found) atomicMin(C.group_found + C.group, (unsigned long long)C.t_blk);
 }
 
-template <int F, int LAYOUT, bool COUNT>
-__global__ void __launch_bounds__(512) es_scan_kernel(const __grid_constant__ EsLaunch L) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ EsInst si;
-    __shared__ unsigned long long s_unit;
-    __shared__ uint32_t s_item;
-    __shared__ int s_skip;
+// warp-uniform: run the tail on up to 32 queued candidates
+template <bool COUNT>
+__device__ __forceinline__ void flush(const TailCtx& C, EsQueue* Q, uint32_t lane, uint32_t& qhead,
+                                      uint32_t& qsize) {
+    __syncwarp();
+    const uint32_t n = qsize < 32u ? qsize : 32u;
+    if (lane < n) {
+        const uint32_t e = (qhead + lane) & (ES_QCAP - 1);
+        tail_one<COUNT>(C, u4(Q->s[e]), Q->idx[e]);
+    }
+    qhead = (qhead + n) & (ES_QCAP - 1);
+    qsize -= n;
+    __syncwarp();
+}
 
-    const uint32_t tid = threadIdx.x;
-    const uint32_t lane = tid & 31u;
-    uint32_t* sm_cnt = reinterpret_cast<uint32_t*>(smem + L.cnt_off);
-    uint32_t* sm_tc = reinterpret_cast<uint32_t*>(smem + L.tconst_off);
-    uint32_t* sm_fast = reinterpret_cast<uint32_t*>(smem + L.fast_off);
-    uint32_t cur_inst = 0xffffffffu, cur_item = 0xffffffffu;
-    const EsItem* items = L.items ? L.items : &L.item0;
-
-    for (;;) {
-        if (tid == 0) {
-            const unsigned long long u = atomicAdd(L.unit_counter, 1ull);
-            uint32_t it = 0;
-            int skip = 0;
-            if (u < L.total_units) {
-                uint32_t lo = 0, hi = L.n_items;
-                while (hi - lo > 1) {
-                    const uint32_t mid = (lo + hi) >> 1;
-                    if (items[mid].unit_begin <= u) lo = mid; else hi = mid;
-                }
-                it = lo;
-                if (L.group_found) {
-                    const unsigned long long fnd =
-                        *reinterpret_cast<volatile unsigned long long*>(L.group_found + items[lo].group);
-                    if (items[lo].t > fnd) skip = 1;
-                }
-            }
-            s_unit = u;
-            s_item = it;
-            s_skip = skip;
-        }
-        __syncthreads();
-        const unsigned long long u = s_unit;
-        if (u >= L.total_units) break;
-        const uint32_t item_id = s_item;
-        if (s_skip) {
-            __syncthreads();
-            continue;
-        }
-        const EsItem& item = items[item_id];
-        const uint32_t* tc_src = L.items ? item.tconst : L.tconst0;
-        // ---- stage the instance tables (on change) and the block constants -------------
-        if (item.inst_id != cur_inst) {
-            if (tid == 0) si = *item.inst;
-            __syncthreads();
-            copy_words(reinterpret_cast<uint32_t*>(smem), reinterpret_cast<const uint32_t*>(si.small),
-                       si.small_bytes >> 2);
-            if (item.sm_fast_words)
-                copy_words(sm_fast, LAYOUT == ES_LAYOUT_WORDMASK ? si.masks : si.allowed,
-                           item.sm_fast_words);
-        }
-        if (item.inst_id != cur_inst || item_id != cur_item) {
-            for (uint32_t f = tid; f < si.n_filters; f += blockDim.x) sm_tc[f] = tc_src[f];
-        }
-        if (COUNT)
-            for (uint32_t f = tid; f < si.n_filters; f += blockDim.x) sm_cnt[f] = 0u;
-        cur_inst = item.inst_id;
-        cur_item = item_id;
-        __syncthreads();
-
-        const EsInst& I = si;
-        EsSmemView V;
-        V.T1 = reinterpret_cast<const ulonglong2*>(smem + I.o_T1);
-        V.TQ1 = reinterpret_cast<const uint32_t*>(smem + I.o_TQ1);
-        V.D2 = reinterpret_cast<const ulonglong2*>(smem + I.o_D2);
-        V.DQ2 = reinterpret_cast<const uint32_t*>(smem + I.o_DQ2);
-        V.S0 = reinterpret_cast<const ulonglong2*>(smem + I.o_S0);
-        V.K0 = reinterpret_cast<const uint32_t*>(smem + I.o_K0);
-        V.I0 = reinterpret_cast<const uint32_t*>(smem + I.o_I0);
-        V.Q0 = reinterpret_cast<const uint32_t*>(smem + I.o_Q0);
-        V.BK = reinterpret_cast<const uint16_t*>(smem + I.o_BK);
-        V.FC = reinterpret_cast<const EsFilterC*>(smem + I.o_FC);
-        V.tc = sm_tc;
-        V.fast = sm_fast;
-
-        const u128 M = mk128(I.M_lo, I.M_hi);
-        const uint32_t r0 = I.r0, r1 = I.r1, r2 = I.r2, W = I.W;
-        uint32_t Feff = (uint32_t)F < L.mask_filters ? (uint32_t)F : L.mask_filters;
-        if (Feff > I.n_filters) Feff = I.n_filters;
-        if (LAYOUT == ES_LAYOUT_WORDMASK && Feff > I.F_built) Feff = I.F_built;
-        const uint32_t n_sm = item.n_sm;
-        uint32_t qf[F], corr[F];
+// warp-uniform: queue the set bits of one inner word (sorted slots base + i)
+template <bool COUNT>
+__device__ __forceinline__ void push(const TailCtx& C, EsQueue* Q, uint32_t lane, uint32_t& qhead,
+                                     uint32_t& qsize, uint32_t bits, uint32_t base, const U4 b,
+                                     uint64_t obase, const uint4* sS0, const uint32_t* sI0) {
+    const uint32_t n = __popc(bits);
+    uint32_t incl = n;
 #pragma unroll
-        for (int f = 0; f < F; ++f) {
-            const bool on = (uint32_t)f < Feff;
-            qf[f] = on ? V.FC[f].q : 1u;
-            corr[f] = on ? V.FC[f].corr : 0u;
+    for (uint32_t o = 1; o < 32; o <<= 1) {
+        const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    const uint32_t tot = __shfl_sync(0xffffffffu, incl, 31);
+    if (qsize + tot > ES_QCAP)
+        while (qsize) flush<COUNT>(C, Q, lane, qhead, qsize);
+    if (tot > ES_QCAP) {
+        // survivor-dense plans (tiny k): tail in place
+        while (bits) {
+            const uint32_t i = __ffs(bits) - 1u;
+            bits &= bits - 1u;
+            const uint32_t slot = base + i;
+            uint32_t wm;
+            const U4 s = addmod(b, u4(sS0[slot]), C.M, wm);
+            tail_one<COUNT>(C, s, obase + sI0[slot]);
         }
-        uint32_t cnt[F];
-#pragma unroll
-        for (int f = 0; f < F; ++f) cnt[f] = 0u;
+        return;
+    }
+    uint32_t pos = qhead + qsize + incl - n;
+    while (bits) {
+        const uint32_t i = __ffs(bits) - 1u;
+        bits &= bits - 1u;
+        const uint32_t slot = base + i;
+        uint32_t wm;
+        const U4 s = addmod(b, u4(sS0[slot]), C.M, wm);
+        const uint32_t qe = pos & (ES_QCAP - 1);
+        Q->s[qe] = make_uint4(s.x, s.y, s.z, s.w);
+        Q->idx[qe] = obase + sI0[slot];
+        ++pos;
+    }
+    qsize += tot;
+    while (qsize >= 32u) flush<COUNT>(C, Q, lane, qhead, qsize);
+}
 
-        // ---- this thread's strip of ring-1 cycles (or list entries) ---------------------
-        const uint64_t rel = (u - item.unit_begin) * L.cycles_per_unit + (uint64_t)tid * L.strip;
-        const bool listed = item.list != nullptr;
-        uint64_t e_lo, e_hi;
-        if (listed) {
-            e_lo = item.o_begin + rel;
-            e_hi = e_lo + L.strip;
-            if (e_hi > item.o_end) e_hi = item.o_end;
-        } else {
-            e_lo = item.c_begin + rel;
-            e_hi = e_lo + L.strip;
-            if (e_hi > item.c_end) e_hi = item.c_end;
-        }
-        u128 b2 = 0;
-        uint32_t d2 = 0;
-        uint32_t BQ2[F];
+// Warp-uniform: scan one warp-unit w of `item`, whose plan is staged in smem / si.
+template <int F, int LAYOUT, bool COUNT, int WT>
+__device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, unsigned char* smem,
+                                          const uint32_t* sm_fast, EsQueue* Q, uint32_t* wcnt,
+                                          uint32_t wcnt_saddr, uint32_t lane, unsigned long long w,
+                                          const EsItem& item, uint32_t item_id) {
+    TailCtx C;
+    C.M = U4{(uint32_t)si.M_lo, (uint32_t)(si.M_lo >> 32), (uint32_t)si.M_hi, (uint32_t)(si.M_hi >> 32)};
+    C.M_lo = si.M_lo;
+    C.kp1 = si.k + 1u;
+    C.M_big = (si.M_hi != 0) || (si.M_lo > C.kp1);
+    C.nf = si.n_filters;
+    C.sFC = reinterpret_cast<const EsFilterC*>(smem + si.o_FC);
+    C.tc = L.items ? item.tconst : L.tconst0;
+    C.allowed_g = si.allowed;
+    C.surv = L.surv;
+    C.surv_n = L.surv_n;
+    C.group_found = L.group_found;
+    C.surv_cap = L.surv_cap;
+    C.wcnt_saddr = wcnt_saddr;
+    C.item_id = item_id;
+    C.group = item.group;
+    C.t_blk = item.t;
+    const U4 M = C.M;
+    const uint32_t r0 = si.r0, r1 = si.r1, r2 = si.r2;
+    const uint32_t Wn = WT ? (uint32_t)WT : si.W;
+    const uint32_t bsh = si.bsh, tail = si.tail_mask;
+    const uint32_t kl = si.sh >> 5, ko = si.sh & 31u;   // key = 32 bits of thr from bit sh
+    const uint32_t* __restrict__ masks_g = si.masks;
+    const uint4* sT1 = reinterpret_cast<const uint4*>(smem + si.o_T1);
+    const uint4* sTQ1 = reinterpret_cast<const uint4*>(smem + si.o_TQ1);
+    const uint4* sD2 = reinterpret_cast<const uint4*>(smem + si.o_D2);
+    const uint4* sDQ2 = reinterpret_cast<const uint4*>(smem + si.o_DQ2);
+    const uint4* sS0 = reinterpret_cast<const uint4*>(smem + si.o_S0);
+    const uint32_t* sK0 = reinterpret_cast<const uint32_t*>(smem + si.o_K0);
+    const uint32_t* sI0 = reinterpret_cast<const uint32_t*>(smem + si.o_I0);
+    const uint32_t* sQ0 = reinterpret_cast<const uint32_t*>(smem + si.o_Q0);
+    const uint16_t* sBK = reinterpret_cast<const uint16_t*>(smem + si.o_BK);
+    const uint64_t ob = item.o_begin, oe = item.o_end;
+    const uint64_t* list = item.list;
+    const uint32_t n_sm = item.n_sm;
+    uint32_t Feff = (uint32_t)F < L.mask_filters ? (uint32_t)F : L.mask_filters;
+    if (Feff > C.nf) Feff = C.nf;
+    if (LAYOUT == ES_LAYOUT_WORDMASK && Feff > si.F_built) Feff = si.F_built;
+    C.Feff = Feff;
+    uint32_t qf[F], corr[F], moff[F];
 #pragma unroll
-        for (int f = 0; f < F; ++f) BQ2[f] = 0u;
-        bool have = false;
-        uint64_t prev_c = 0;
+    for (int f = 0; f < F; ++f) {
+        const bool on = (uint32_t)f < Feff;
+        qf[f] = on ? C.sFC[f].q : 1u;
+        corr[f] = on ? C.sFC[f].corr : 0u;
+        moff[f] = LAYOUT == ES_LAYOUT_WORDMASK ? si.mask_off[f] : (on ? C.sFC[f].off : 0u);
+    }
+    uint32_t cnt[F];
+#pragma unroll
+    for (int f = 0; f < F; ++f) cnt[f] = 0u;
+    uint32_t qhead = 0, qsize = 0;
 
-        // Every lane runs L.strip iterations so the warp-wide ballots below see all 32 lanes;
-        // lanes past the end of their strip take part with an empty candidate set.
-        for (uint32_t step = 0; step < L.strip; ++step) {
-            const uint64_t e = e_lo + step;
-            const bool live = e < e_hi;
-            if (__ballot_sync(0xffffffffu, live) == 0u) break;
-            uint64_t c = prev_c;
-            uint32_t lo1 = 0u, hi1 = 0u;
-            if (!live) {
-                // keep the decoded state; no positions
-            } else if (listed) {
-                const uint64_t o = __ldg(reinterpret_cast<const unsigned long long*>(item.list) + e);
+    const uint64_t rel = (w - item.unit_begin) * 32ull * L.strip + (uint64_t)lane * L.strip;
+    uint64_t e_lo, e_hi;
+    if (list) {
+        e_lo = ob + rel;
+        e_hi = e_lo + L.strip;
+        if (e_hi > oe) e_hi = oe;
+    } else {
+        e_lo = item.c_begin + rel;
+        e_hi = e_lo + L.strip;
+        if (e_hi > item.c_end) e_hi = item.c_end;
+    }
+    U4 b2{0u, 0u, 0u, 0u};
+    uint32_t d2 = 0;
+    uint32_t BQ2[F];
+#pragma unroll
+    for (int f = 0; f < F; ++f) BQ2[f] = 0u;
+    bool have = false;
+    uint64_t prev_c = 0;
+    // every lane runs L.strip steps so the warp-wide votes below see 32 lanes
+    for (uint32_t step = 0; step < L.strip; ++step) {
+        const uint64_t e = e_lo + step;
+        const bool live = e < e_hi;
+        if (__ballot_sync(0xffffffffu, live) == 0u) break;
+        uint64_t c = prev_c;
+        uint32_t lo1 = 0u, hi1 = 0u;
+        if (live) {
+            if (list) {
+                const uint64_t o = __ldg(reinterpret_cast<const unsigned long long*>(list) + e);
                 c = o / r1;
                 lo1 = (uint32_t)(o - c * r1);
                 hi1 = lo1 + 1u;
             } else {
                 c = e;
                 const uint64_t o0 = c * r1;
-                lo1 = item.o_begin > o0 ? (uint32_t)(item.o_begin - o0) : 0u;
-                const uint64_t span = item.o_end - o0;
+                lo1 = ob > o0 ? (uint32_t)(ob - o0) : 0u;
+                const uint64_t span = oe - o0;
                 hi1 = span < r1 ? (uint32_t)span : r1;
             }
-            // ---- rings >= 2: decode at strip start / ring-3 carry, else one delta step ----
-            if (!live) {
-            } else if (have && c == prev_c + 1 && d2 + 1u < r2) {
-                uint32_t w;
-                b2 = addmod(b2, mk128(V.D2[d2].x, V.D2[d2].y), M, w);
+            // rings >= 2: one delta step while the ring-2 digit advances, else a decode
+            if (have && c == prev_c + 1 && d2 + 1u < r2) {
+                uint32_t wm;
+                b2 = addmod(b2, u4(sD2[d2]), M, wm);
 #pragma unroll
-                for (int f = 0; f < F; ++f)
-                    BQ2[f] = red2(BQ2[f] + V.DQ2[d2 * ES_FMAX + f] + (w ? corr[f] : 0u), qf[f]);
+                for (int g = 0; g < F; g += 4) {
+                    const uint4 dq = sDQ2[d2 * (ES_FMAX / 4) + (g >> 2)];
+#pragma unroll
+                    for (int h = 0; h < 4 && g + h < F; ++h) {
+                        const uint32_t dv = h == 0 ? dq.x : (h == 1 ? dq.y : (h == 2 ? dq.z : dq.w));
+                        BQ2[g + h] = red2(BQ2[g + h] + dv + (corr[g + h] & wm), qf[g + h]);
+                    }
+                }
                 ++d2;
             } else if (!(have && c == prev_c)) {
-                b2 = decode_cycle(I, c, M, d2);
+                b2 = decode_cycle(si, c, M, d2);
 #pragma unroll
                 for (int f = 0; f < F; ++f) {
-                    if ((uint32_t)f < Feff) {
-                        uint32_t v = mod128(b2, V.FC[f]) + V.tc[f];
-                        BQ2[f] = v >= qf[f] ? v - qf[f] : v;
-                    }
+                    if ((uint32_t)f < Feff) BQ2[f] = red1(mod128(b2, C.sFC[f]) + C.tc[f], qf[f]);
                 }
                 have = true;
             }
             prev_c = c;
+        }
 
-            // ---- ring 1: warp-uniform sweep --------------------------------------------
-            for (uint32_t d1 = 0; d1 < r1; ++d1) {
-                const bool act = (d1 >= lo1) && (d1 < hi1);
-                const ulonglong2 tv = V.T1[d1];
-                uint32_t w1;
-                const u128 b = addmod(b2, mk128(tv.x, tv.y), M, w1);
-                uint32_t BQ[F];
-#pragma unroll
-                for (int f = 0; f < F; ++f)
-                    BQ[f] = red2(BQ2[f] + V.TQ1[d1 * ES_FMAX + f] + (w1 ? corr[f] : 0u), qf[f]);
-                // carry split: slots [split, r0) wrap past M
-                const u128 thr = M - b;
-                const uint32_t t32 = (uint32_t)(thr >> I.sh);
-                uint32_t split = V.BK[t32 >> I.bsh];
-                while (split < r0 && V.K0[split] < t32) ++split;
-                while (split < r0 && V.K0[split] == t32 &&
-                       mk128(V.S0[split].x, V.S0[split].y) < thr)
-                    ++split;
-                const uint64_t oidx = c * r1 + d1;
+        // ---- ring 1: warp-uniform sweep (broadcast loads) --------------------------------
+        for (uint32_t d1 = 0; d1 < r1; ++d1) {
+            const bool act = (d1 >= lo1) && (d1 < hi1);
+            uint32_t wm1;
+            const U4 b = addmod(b2, u4(sT1[d1]), M, wm1);
+            const uint32_t* tq_row = reinterpret_cast<const uint32_t*>(sTQ1 + d1 * (ES_FMAX / 4));
+            // carry split: sorted slots [split, r0) wrap past M (sentinels at r0)
+            uint32_t brw;
+            const U4 thr = sub128(M, b, brw);
+            const uint32_t klo = kl == 0 ? thr.x : (kl == 1 ? thr.y : thr.z);
+            const uint32_t khi = kl == 0 ? thr.y : (kl == 1 ? thr.z : thr.w);
+            const uint32_t t32 = __funnelshift_r(klo, khi, ko);
+            uint32_t split = sBK[t32 >> bsh];
+            split += (sK0[split] < t32) ? 1u : 0u;
+            split += (sK0[split] < t32) ? 1u : 0u;
+            if (sK0[split] <= t32) {
+                while (sK0[split] < t32) ++split;
+                while (sK0[split] == t32 && lt128(u4(sS0[split]), thr)) ++split;
+            }
 
-                for (uint32_t wd = 0; wd < W; ++wd) {
-                    const uint32_t valid = (wd + 1u == W) ? I.tail_mask : 0xffffffffu;
-                    uint32_t bits = act ? valid : 0u;
-                    const uint32_t base = wd << 5;
-                    const uint32_t cm = split <= base ? valid
-                                      : (split >= base + 32u ? 0u : ((0xffffffffu << (split - base)) & valid));
+            for (uint32_t wd = 0; wd < Wn; ++wd) {
+                const uint32_t valid = (wd + 1u == Wn) ? tail : 0xffffffffu;
+                uint32_t bits = act ? valid : 0u;
+                const uint32_t base = wd << 5;
+                const uint32_t cm = split <= base ? valid
+                                  : (split >= base + 32u ? 0u : ((0xffffffffu << (split - base)) & valid));
+                bool alive = true;   // warp-uniform: some lane still has a live candidate
 #pragma unroll
-                    for (int f = 0; f < F; ++f) {
-                        if ((uint32_t)f < Feff) {
-                            if (LAYOUT == ES_LAYOUT_WORDMASK) {
-                                const uint32_t ph0 = BQ[f];
-                                uint32_t ph1 = ph0 + corr[f];
-                                ph1 = ph1 >= qf[f] ? ph1 - qf[f] : ph1;
-                                uint32_t m0, m1;
-                                if ((uint32_t)f < n_sm) {
-                                    const uint32_t* tab = V.fast + I.mask_off[f];
-                                    m0 = tab[ph0 * W + wd];
-                                    m1 = tab[ph1 * W + wd];
-                                } else {
-                                    const uint32_t* tab = I.masks + I.mask_off[f];
-                                    m0 = __ldg(tab + ph0 * W + wd);
-                                    m1 = __ldg(tab + ph1 * W + wd);
-                                }
-                                bits &= (m0 & ~cm) | (m1 & cm);
+                for (int f = 0; f < F; ++f) {
+                    if (alive && (uint32_t)f < Feff) {
+                        // n mod q_f for the ring-0 base of this outer index
+                        const uint32_t bqf = red2(BQ2[f] + tq_row[f] + (corr[f] & wm1), qf[f]);
+                        if (LAYOUT == ES_LAYOUT_WORDMASK) {
+                            const uint32_t x0 = bqf;
+                            const uint32_t x1 = red1(x0 + corr[f], qf[f]);
+                            uint32_t m0, m1;
+                            if ((uint32_t)f < n_sm) {
+                                const uint32_t* tab = sm_fast + moff[f] + wd;
+                                m0 = tab[x0 * Wn];
+                                m1 = tab[x1 * Wn];
                             } else {
-                                const uint32_t* tab = ((uint32_t)f < n_sm) ? (V.fast + V.FC[f].off)
-                                                                           : (I.allowed + V.FC[f].off);
-                                uint32_t nb = 0u, live = bits;
-                                while (live) {
-                                    const uint32_t i = __ffs(live) - 1u;
-                                    live &= live - 1u;
-                                    const uint32_t slot = base + i;
-                                    const uint32_t m = red2(BQ[f] + V.Q0[f * r0 + slot] +
-                                                                ((slot >= split) ? corr[f] : 0u),
-                                                            qf[f]);
-                                    const uint32_t wv = ((uint32_t)f < n_sm) ? tab[m >> 5] : __ldg(tab + (m >> 5));
-                                    nb |= ((wv >> (m & 31u)) & 1u) << i;
-                                }
-                                bits = nb;
+                                const uint32_t* tab = masks_g + moff[f] + wd;
+                                m0 = __ldg(tab + x0 * Wn);
+                                m1 = __ldg(tab + x1 * Wn);
                             }
-                            if (COUNT) cnt[f] += __popc(bits);
+                            bits &= (m0 & ~cm) | (m1 & cm);
+                        } else {
+                            uint32_t nb = 0u, live_bits = bits;
+                            while (live_bits) {
+                                const uint32_t i = __ffs(live_bits) - 1u;
+                                live_bits &= live_bits - 1u;
+                                const uint32_t slot = base + i;
+                                const uint32_t m = red2(bqf + sQ0[f * r0 + slot] + ((slot >= split) ? corr[f] : 0u), qf[f]);
+                                const uint32_t wv = ((uint32_t)f < n_sm) ? sm_fast[moff[f] + (m >> 5)]
+                                                                         : __ldg(C.allowed_g + moff[f] + (m >> 5));
+                                nb |= ((wv >> (m & 31u)) & 1u) << i;
+                            }
+                            bits = nb;
                         }
-                        if (__ballot_sync(0xffffffffu, bits != 0u) == 0u) break;
+                        if (COUNT) cnt[f] += __popc(bits);
+                        if (f + 1 < F && (uint32_t)(f + 1) < Feff) alive = __ballot_sync(0xffffffffu, bits != 0u) != 0u;
                     }
-                    // ---- survivors of the inner-ring stage: exact tail of the cascade ----
-                    while (bits) {
-                        const uint32_t i = __ffs(bits) - 1u;
-                        bits &= bits - 1u;
-                        const uint32_t slot = base + i;
-                        u128 s = b + mk128(V.S0[slot].x, V.S0[slot].y);
-                        if (slot >= split) s -= M;
-                        if (tail_filters<COUNT>(V, I, Feff, s, sm_cnt)) {
-                            emit<COUNT>(L, item, I, item_id, oidx * (uint64_t)r0 + V.I0[slot], s, M);
-                        }
+                }
+                // ---- queue the survivors of the inner-ring stage -----------------------------
+                if (__ballot_sync(0xffffffffu, bits != 0u))
+                    push<COUNT>(C, Q, lane, qhead, qsize, bits, base, b, (c * r1 + d1) * (uint64_t)r0, sS0, sI0);
+            }
+        }
+    }
+    while (qsize) flush<COUNT>(C, Q, lane, qhead, qsize);
+    // ---- per-stage counts of this warp-unit into the item's totals ----------------------
+    if (COUNT) {
+        unsigned long long* gc = item.counts;
+#pragma unroll
+        for (int f = 0; f < F; ++f) {
+            const uint32_t v = __reduce_add_sync(0xffffffffu, cnt[f]);
+            if (lane == 0 && v && gc) atomicAdd(gc + f, (unsigned long long)v);
+        }
+        __syncwarp();
+        for (uint32_t f = Feff + lane; f < C.nf; f += 32u) {
+            const uint32_t v = wcnt[f];
+            if (v) {
+                if (gc) atomicAdd(gc + f, (unsigned long long)v);
+                wcnt[f] = 0u;
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// Work distribution.  A warp-unit is 32 lanes x `strip` consecutive ring-1 cycles (or list
+// entries) of one item.  Direct mode (every item of the launch uses one plan): the CTA stages
+// the plan's tables once, then each warp claims warp-units from the global counter on its own --
+// no CTA barrier after staging.  Chunk mode (several plans): a CTA claims a chunk of
+// warp-units, restages when the plan changes, and its warps claim the chunk's units from a
+// shared counter; the only barriers are at chunk/item boundaries.
+//
+// Template: F = filters evaluated in the inner-ring stage (upper bound, runtime Feff <= F),
+// LAYOUT = word-mask or scalar tables, COUNT = per-stage pass counts, WT = words per inner ring
+// when known at compile time (1: r0 <= 32, 2: r0 <= 64), 0 = runtime.
+template <int F, int LAYOUT, bool COUNT, int WT>
+__global__ void __launch_bounds__(ES_LB_THREADS, ES_LB_MINB) es_scan_kernel(const __grid_constant__ EsLaunch L) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ EsInst si;
+    __shared__ unsigned long long s_u0, s_u1, s_end, s_next;
+    __shared__ uint32_t s_item;
+    __shared__ int s_skip;
+
+    const uint32_t tid = threadIdx.x;
+    const uint32_t lane = tid & 31u;
+    const uint32_t warp = tid >> 5;
+    uint32_t* sm_fast = reinterpret_cast<uint32_t*>(smem + L.fast_off);
+    EsQueue* Q = reinterpret_cast<EsQueue*>(smem + L.queue_off) + warp;
+    uint32_t* wcnt = reinterpret_cast<uint32_t*>(smem + L.cnt_off) + warp * L.nf_max;
+    const uint32_t wcnt_saddr = (uint32_t)__cvta_generic_to_shared(wcnt);
+    const EsItem* items = L.items ? L.items : &L.item0;
+    const unsigned long long total = L.total_units;
+
+    if (COUNT)
+        for (uint32_t f = lane; f < L.nf_max; f += 32u) wcnt[f] = 0u;
+
+    if (L.direct) {
+        // ---- stage the one plan, then warps claim warp-units on their own ---------------
+        if (tid == 0) si = *items[0].inst;
+        __syncthreads();
+        copy_words(reinterpret_cast<uint32_t*>(smem), reinterpret_cast<const uint32_t*>(si.small), si.small_bytes >> 2);
+        if (items[0].sm_fast_words)
+            copy_words(const_cast<uint32_t*>(sm_fast), LAYOUT == ES_LAYOUT_WORDMASK ? si.masks : si.allowed,
+                       items[0].sm_fast_words);
+        __syncthreads();
+        for (;;) {
+            unsigned long long w = 0;
+            uint32_t it_id = 0;
+            int skip = 0;
+            if (lane == 0) {
+                w = atomicAdd(L.unit_counter, 1ull);
+                if (w < total) {
+                    uint32_t lo = 0, hi = L.n_items;
+                    while (hi - lo > 1) {
+                        const uint32_t mid = (lo + hi) >> 1;
+                        if (items[mid].unit_begin <= w) lo = mid; else hi = mid;
+                    }
+                    it_id = lo;
+                    if (L.group_found) {
+                        const unsigned long long fnd =
+                            *reinterpret_cast<volatile unsigned long long*>(L.group_found + items[lo].group);
+                        if (items[lo].t > fnd) skip = 1;
                     }
                 }
             }
+            w = __shfl_sync(0xffffffffu, w, 0);
+            if (w >= total) break;
+            it_id = __shfl_sync(0xffffffffu, it_id, 0);
+            skip = __shfl_sync(0xffffffffu, skip, 0);
+            if (skip) continue;
+            scan_unit<F, LAYOUT, COUNT, WT>(L, si, smem, sm_fast, Q, wcnt, wcnt_saddr, lane, w, items[it_id], it_id);
         }
-        // ---- flush per-stage counts ------------------------------------------------------
-        if (COUNT) {
-#pragma unroll
-            for (int f = 0; f < F; ++f) {
-                const uint32_t v = __reduce_add_sync(0xffffffffu, cnt[f]);
-                if (lane == 0 && v) atomicAdd(sm_cnt + f, v);
-            }
-            __syncthreads();
-            if (item.counts)
-                for (uint32_t f = tid; f < I.n_filters; f += blockDim.x)
-                    if (sm_cnt[f]) atomicAdd(item.counts + f, (unsigned long long)sm_cnt[f]);
+        return;
+    }
+
+    uint32_t cur_inst = 0xffffffffu;
+    for (;;) {
+        // ---- CTA claims a chunk of warp-units; the size shrinks as the work runs out ---------
+        if (tid == 0) {
+            const unsigned long long cur = *reinterpret_cast<volatile unsigned long long*>(L.unit_counter);
+            const unsigned long long rem = cur < total ? total - cur : 0ull;
+            unsigned long long ch = rem / (2ull * gridDim.x);
+            if (ch < 1ull) ch = 1ull;
+            if (ch > (unsigned long long)L.chunk_max) ch = L.chunk_max;
+            const unsigned long long u0 = atomicAdd(L.unit_counter, ch);
+            s_u0 = u0;
+            s_u1 = (u0 + ch < total) ? u0 + ch : total;
         }
         __syncthreads();
+        const unsigned long long u1 = s_u1;
+        unsigned long long u = s_u0;
+        if (u >= total) break;
+        while (u < u1) {
+            if (tid == 0) {
+                uint32_t lo = 0, hi = L.n_items;
+                while (hi - lo > 1) {
+                    const uint32_t mid = (lo + hi) >> 1;
+                    if (items[mid].unit_begin <= u) lo = mid; else hi = mid;
+                }
+                const EsItem& it = items[lo];
+                unsigned long long e = it.unit_begin + it.n_units;
+                if (e > u1) e = u1;
+                int skip = 0;
+                if (L.group_found) {
+                    const unsigned long long fnd =
+                        *reinterpret_cast<volatile unsigned long long*>(L.group_found + it.group);
+                    if (it.t > fnd) skip = 1;
+                }
+                s_item = lo;
+                s_end = e;
+                s_next = u;
+                s_skip = skip;
+            }
+            __syncthreads();
+            const uint32_t item_id = s_item;
+            const unsigned long long end = s_end;
+            if (!s_skip) {
+                const EsItem& item = items[item_id];
+                if (item.inst_id != cur_inst) {
+                    // restage: the header, small tables and this plan's staged fast tables
+                    if (tid == 0) si = *item.inst;
+                    __syncthreads();
+                    copy_words(reinterpret_cast<uint32_t*>(smem), reinterpret_cast<const uint32_t*>(si.small),
+                               si.small_bytes >> 2);
+                    if (item.sm_fast_words)
+                        copy_words(const_cast<uint32_t*>(sm_fast), LAYOUT == ES_LAYOUT_WORDMASK ? si.masks : si.allowed,
+                                   item.sm_fast_words);
+                    __syncthreads();
+                    cur_inst = item.inst_id;
+                }
+                for (;;) {
+                    unsigned long long w = 0;
+                    if (lane == 0) w = atomicAdd(&s_next, 1ull);
+                    w = __shfl_sync(0xffffffffu, w, 0);
+                    if (w >= end) break;
+                    scan_unit<F, LAYOUT, COUNT, WT>(L, si, smem, sm_fast, Q, wcnt, wcnt_saddr, lane, w, item, item_id);
+                }
+            }
+            __syncthreads();
+            u = end;
+        }
     }
 }
 
@@ -491,18 +697,24 @@ __global__ void __launch_bounds__(256) es_int_peak_kernel(unsigned long long* si
 
 typedef void (*ScanFn)(const EsLaunch);
 
-template <int LAYOUT, bool COUNT>
+template <int LAYOUT, bool COUNT, int WT>
 ScanFn pick_f(uint32_t f) {
-    if (f <= 2) return es_scan_kernel<2, LAYOUT, COUNT>;
-    if (f <= 4) return es_scan_kernel<4, LAYOUT, COUNT>;
-    if (f <= 6) return es_scan_kernel<6, LAYOUT, COUNT>;
-    return es_scan_kernel<8, LAYOUT, COUNT>;
+    if (f <= 2) return es_scan_kernel<2, LAYOUT, COUNT, WT>;
+    if (f <= 4) return es_scan_kernel<4, LAYOUT, COUNT, WT>;
+    if (f <= 6) return es_scan_kernel<6, LAYOUT, COUNT, WT>;
+    return es_scan_kernel<8, LAYOUT, COUNT, WT>;
 }
 
-ScanFn pick(int layout, int count, uint32_t f) {
-    if (layout == ES_LAYOUT_WORDMASK)
-        return count ? pick_f<ES_LAYOUT_WORDMASK, true>(f) : pick_f<ES_LAYOUT_WORDMASK, false>(f);
-    return count ? pick_f<ES_LAYOUT_SCALAR, true>(f) : pick_f<ES_LAYOUT_SCALAR, false>(f);
+template <bool COUNT>
+ScanFn pick_w(int layout, uint32_t words, uint32_t f) {
+    if (layout == ES_LAYOUT_SCALAR) return pick_f<ES_LAYOUT_SCALAR, COUNT, 0>(f);
+    if (words == 1) return pick_f<ES_LAYOUT_WORDMASK, COUNT, 1>(f);
+    if (words == 2) return pick_f<ES_LAYOUT_WORDMASK, COUNT, 2>(f);
+    return pick_f<ES_LAYOUT_WORDMASK, COUNT, 0>(f);
+}
+
+ScanFn pick(int layout, int count, uint32_t words, uint32_t f) {
+    return count ? pick_w<true>(layout, words, f) : pick_w<false>(layout, words, f);
 }
 
 }  // namespace
@@ -510,25 +722,27 @@ ScanFn pick(int layout, int count, uint32_t f) {
 // Raise the dynamic shared-memory limit of every scan instance once per process/device.
 int es_scan_prepare(int smem_optin_bytes) {
     const uint32_t fs[4] = {2, 4, 6, 8};
+    const uint32_t ws[3] = {1, 2, 3};
     for (int layout = 0; layout < 2; ++layout)
         for (int count = 0; count < 2; ++count)
-            for (uint32_t f : fs) {
-                cudaError_t e = cudaFuncSetAttribute(pick(layout, count, f),
-                                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                     smem_optin_bytes);
-                if (e != cudaSuccess) return (int)e;
-            }
+            for (uint32_t w : ws)
+                for (uint32_t f : fs) {
+                    cudaError_t e = cudaFuncSetAttribute(pick(layout, count, w, f),
+                                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                         smem_optin_bytes);
+                    if (e != cudaSuccess) return (int)e;
+                }
     return 0;
 }
 
-int es_scan_occupancy(int layout, int count, uint32_t mask_filters, int threads, int smem_bytes,
-                      int* ctas_per_sm) {
+int es_scan_occupancy(int layout, int count, uint32_t words, uint32_t mask_filters, int threads,
+                      int smem_bytes, int* ctas_per_sm) {
     return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        ctas_per_sm, pick(layout, count, mask_filters), threads, (size_t)smem_bytes);
+        ctas_per_sm, pick(layout, count, words, mask_filters), threads, (size_t)smem_bytes);
 }
 
-int es_launch_scan(const EsLaunch& L, int layout, int count, int grid, void* stream) {
-    pick(layout, count, L.mask_filters)<<<grid, L.threads, L.smem_bytes, (cudaStream_t)stream>>>(L);
+int es_launch_scan(const EsLaunch& L, int layout, int count, uint32_t words, int grid, void* stream) {
+    pick(layout, count, words, L.mask_filters)<<<grid, L.threads, L.smem_bytes, (cudaStream_t)stream>>>(L);
     return (int)cudaGetLastError();
 }
 

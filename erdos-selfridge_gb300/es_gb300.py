@@ -47,10 +47,11 @@ TUNABLES = dict(_PLAN_TUNABLES)
 TUNABLES.update({
     "chunk_log2": 34,        # positions per _launch chunk issued by scan_block
     "layout": "wordmask",    # "wordmask" | "scalar"
-    "strip": 4,              # ring-1 cycles per thread per work unit
-    "smem_kb": 200,          # shared-memory budget for staged tables
-    "ctas_per_sm": 2,
-    "count_stages": 1,       # per-filter-stage pass counts
+    "threads": 512,          # CTA size
+    "strip": 2,              # ring-1 cycles per lane per warp-unit
+    "smem_kb": 0,            # shared-memory budget for staged word-mask tables (0: read via L1)
+    "ctas_per_sm": 4,
+    "count_stages": 0,       # per-filter-stage pass counts (es_stage_counts needs 1)
     "search_batch_log2": 34, # positions per multi-block search launch
 })
 
@@ -69,9 +70,9 @@ def _tune_from(tun: dict) -> N.Tune:
     layout = tun.get("layout", "wordmask")
     return N.make_tune(layout=N.LAYOUT_SCALAR if layout == "scalar" else N.LAYOUT_WORDMASK,
                        mask_filters=max(1, min(N.MAX_MASK_FILTERS, int(tun.get("fast_filters", 4)))),
-                       threads=int(tun.get("threads", 256)), strip=int(tun.get("strip", 4)),
-                       smem_kb=int(tun.get("smem_kb", 200)), ctas_per_sm=int(tun.get("ctas_per_sm", 2)),
-                       count_stages=int(tun.get("count_stages", 1)))
+                       threads=int(tun.get("threads", 512)), strip=int(tun.get("strip", 2)),
+                       smem_kb=int(tun.get("smem_kb", 0)), ctas_per_sm=int(tun.get("ctas_per_sm", 4)),
+                       count_stages=int(tun.get("count_stages", 0)))
 
 
 class _Tconst:

@@ -13,7 +13,7 @@ import os
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libes_gb300.so")
+LIB_PATH = os.environ.get("ES_GB300_LIB") or os.path.join(HERE, "libes_gb300.so")
 
 ES_OK = 0
 ES_ERR_OVERFLOW = -3
@@ -159,8 +159,8 @@ class PlanArrays:
                              allowed=_ptr(self.allowed, C.c_uint32))
 
 
-def make_tune(layout=LAYOUT_WORDMASK, mask_filters=4, threads=256, strip=4, smem_kb=200,
-              ctas_per_sm=2, count_stages=1) -> Tune:
+def make_tune(layout=LAYOUT_WORDMASK, mask_filters=4, threads=512, strip=2, smem_kb=0,
+              ctas_per_sm=4, count_stages=1) -> Tune:
     return Tune(layout=int(layout), mask_filters=int(mask_filters), threads=int(threads),
                 strip=int(strip), smem_kb=int(smem_kb), ctas_per_sm=int(ctas_per_sm),
                 count_stages=int(count_stages), reserved=0)
