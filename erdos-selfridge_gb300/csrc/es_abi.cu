@@ -92,11 +92,11 @@ es_tune default_tune() {
     es_tune t;
     t.layout = ES_LAYOUT_WORDMASK;
     t.mask_filters = 4;
-    t.threads = 256;
-    t.strip = 4;
-    t.smem_kb = 200;
-    t.ctas_per_sm = 1;
-    t.count_stages = 1;
+    t.threads = 512;
+    t.strip = 2;
+    t.smem_kb = 0;
+    t.ctas_per_sm = 4;
+    t.count_stages = 0;
     t.reserved = 0;
     return t;
 }
@@ -156,7 +156,8 @@ struct es_batch {
     unsigned long long* d_min = nullptr;
     EsLaunch L{};
     int grid = 0;
-    uint32_t words = 0;  // inner-ring words shared by every plan, 0 when they differ
+    uint32_t words = 0;    // inner-ring words shared by every plan, 0 when they differ
+    uint32_t filters = 0;  // inner-ring stage filters of the launched kernel
     bool ran = false;
 };
 
@@ -192,28 +193,19 @@ SmemPlan plan_smem(uint32_t small_max, uint32_t nf_max, const es_tune& tune, uin
     return p;
 }
 
-// Largest prefix of fast tables (by filter) that fits cap words, among the first F filters.
-void fast_prefix(const es_ctx* c, uint32_t layout, uint32_t F, uint32_t cap, uint32_t* n_sm,
-                 uint32_t* words) {
-    const std::vector<uint32_t>& pre = layout == ES_LAYOUT_WORDMASK ? c->fast_words_mask
-                                                                     : c->fast_words_bits;
-    uint32_t lim = std::min<uint32_t>(F, (uint32_t)pre.size() - 1);
-    uint32_t n = 0;
-    while (n < lim && pre[n + 1] <= cap) ++n;
-    *n_sm = n;
-    *words = pre[n];
+// Filters of the inner-ring stage actually compiled into the launched kernel: word-mask kernels
+// are instantiated for exactly 0..6 and 8 filters (never more than the plan has or the tables
+// built); the scalar layout takes a runtime count.
+uint32_t stage_filters(uint32_t layout, uint32_t requested, uint32_t nf, uint32_t built) {
+    if (layout == ES_LAYOUT_SCALAR) return std::max<uint32_t>(requested, 1);
+    uint32_t f = std::min(std::min(requested, nf), built);
+    return f == 7 ? 6 : f;
 }
 
-uint32_t fast_need(const es_ctx* c, uint32_t layout, uint32_t F) {
-    const std::vector<uint32_t>& pre = layout == ES_LAYOUT_WORDMASK ? c->fast_words_mask
-                                                                     : c->fast_words_bits;
-    return pre[std::min<uint32_t>(F, (uint32_t)pre.size() - 1)];
-}
-
-int grid_for(uint32_t layout, uint32_t count, uint32_t words, const es_tune& tune, uint32_t smem,
-             uint64_t units, int* grid) {
+int grid_for(uint32_t layout, uint32_t count, uint32_t words, uint32_t filters, const es_tune& tune,
+             uint32_t smem, uint64_t units, int* grid) {
     int occ = 0;
-    int e = es_scan_occupancy((int)layout, (int)count, words, tune.mask_filters, (int)tune.threads,
+    int e = es_scan_occupancy((int)layout, (int)count, words, filters, (int)tune.threads,
                               (int)smem, &occ);
     if (e) return cuda_fail((cudaError_t)e, "occupancy");
     if (occ < 1) return fail(ES_ERR_ARG, "launch shape does not fit one SM (threads/smem)");
@@ -586,14 +578,15 @@ static int ctx_launch(es_ctx* c, uint64_t ob, uint64_t oe, const uint64_t* d_lis
     it.n_units = (n_work + per_unit - 1) / per_unit;
     it.group = 0;
     it.inst_id = 0;
-    const uint32_t F = std::min<uint32_t>(tn.mask_filters, std::max<uint32_t>(I.n_filters, 1));
-    const SmemPlan sp = plan_smem((uint32_t)I.small_bytes, I.n_filters, tn, fast_need(c, tn.layout, F));
-    fast_prefix(c, tn.layout, F, sp.fast_words_cap, &it.n_sm, &it.sm_fast_words);
+    const uint32_t F = stage_filters(tn.layout, tn.mask_filters, I.n_filters, I.F_built);
+    const SmemPlan sp = plan_smem((uint32_t)I.small_bytes, I.n_filters, tn, 0);
+    it.n_sm = 0;
+    it.sm_fast_words = 0;
     L.items = nullptr;
     L.n_items = 1;
     L.threads = tn.threads;
     L.strip = tn.strip;
-    L.mask_filters = tn.mask_filters;
+    L.mask_filters = F;
     L.total_units = it.n_units;
     L.chunk_max = 16u * (tn.threads / 32u);
     L.nf_max = std::max<uint32_t>(I.n_filters, 1);
@@ -611,7 +604,7 @@ static int ctx_launch(es_ctx* c, uint64_t ob, uint64_t oe, const uint64_t* d_lis
     memcpy(L.tconst0, c->tconst, 4ull * I.n_filters);
     if (it.n_units == 0) return ES_OK;
     int grid = 0;
-    if (int e = grid_for(tn.layout, tn.count_stages, I.W, tn, sp.bytes, it.n_units, &grid)) return e;
+    if (int e = grid_for(tn.layout, tn.count_stages, I.W, F, tn, sp.bytes, it.n_units, &grid)) return e;
     ES_CUDA(cudaMemsetAsync(c->d_unit, 0, 8, c->stream), "memset");
     int e = es_launch_scan(L, (int)tn.layout, (int)tn.count_stages, I.W, grid, c->stream);
     if (e) return cuda_fail((cudaError_t)e, "scan launch");
@@ -749,16 +742,16 @@ int es_batch_create(es_ctx* const* ctxs, uint32_t n_ctx, const es_batch_item* it
     b->tune = tune;
     b->ctxs.assign(ctxs, ctxs + n_ctx);
     // launch-wide smem plan: the largest small block / filter count, one fast-table budget
-    uint32_t small_max = 0, nf_max = 1, need_max = 0;
+    uint32_t small_max = 0, nf_max = 1, F = tune.mask_filters;
     for (uint32_t i = 0; i < n_ctx; ++i) {
         const es_ctx* c = ctxs[i];
         if (!c) { es_batch_destroy(b); return fail(ES_ERR_ARG, "null context in batch"); }
         small_max = std::max<uint32_t>(small_max, c->h_inst.small_bytes);
         nf_max = std::max<uint32_t>(nf_max, c->h_inst.n_filters);
-        const uint32_t F = std::min<uint32_t>(tune.mask_filters, std::max<uint32_t>(c->h_inst.n_filters, 1));
-        need_max = std::max<uint32_t>(need_max, fast_need(c, tune.layout, F));
+        F = std::min(F, stage_filters(tune.layout, tune.mask_filters, c->h_inst.n_filters, c->h_inst.F_built));
     }
-    const SmemPlan sp = plan_smem(small_max, nf_max, tune, need_max);
+    b->filters = F;
+    const SmemPlan sp = plan_smem(small_max, nf_max, tune, 0);
     const uint64_t per_unit = 32ull * tune.strip;
     b->words = ctxs[0]->h_inst.W;
     for (uint32_t i = 1; i < n_ctx; ++i)
@@ -792,8 +785,8 @@ int es_batch_create(es_ctx* const* ctxs, uint32_t n_ctx, const es_batch_item* it
         units += it.n_units;
         it.group = s.group;
         it.inst_id = s.ctx_index;
-        const uint32_t F = std::min<uint32_t>(tune.mask_filters, std::max<uint32_t>(I.n_filters, 1));
-        fast_prefix(c, tune.layout, F, sp.fast_words_cap, &it.n_sm, &it.sm_fast_words);
+        it.n_sm = 0;
+        it.sm_fast_words = 0;
         // per-block constants tconst[j] = (t mod q)(M mod q) mod q
         it.tconst = reinterpret_cast<const uint32_t*>((uintptr_t)h_tc.size());  // patched below
         for (uint32_t f = 0; f < I.n_filters; ++f) {
@@ -838,7 +831,7 @@ int es_batch_create(es_ctx* const* ctxs, uint32_t n_ctx, const es_batch_item* it
     L.n_items = n_items;
     L.threads = tune.threads;
     L.strip = tune.strip;
-    L.mask_filters = tune.mask_filters;
+    L.mask_filters = F;
     L.total_units = units;
     L.chunk_max = 16u * (tune.threads / 32u);
     L.nf_max = nf_max;
@@ -853,7 +846,7 @@ int es_batch_create(es_ctx* const* ctxs, uint32_t n_ctx, const es_batch_item* it
     L.fast_off = sp.fast_off;
     L.cnt_off = sp.cnt_off;
     L.queue_off = sp.queue_off;
-    if (int e = grid_for(tune.layout, tune.count_stages, b->words, tune, sp.bytes, std::max<uint64_t>(units, 1), &b->grid)) {
+    if (int e = grid_for(tune.layout, tune.count_stages, b->words, F, tune, sp.bytes, std::max<uint64_t>(units, 1), &b->grid)) {
         es_batch_destroy(b);
         return e;
     }

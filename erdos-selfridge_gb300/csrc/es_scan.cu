@@ -159,6 +159,19 @@ __device__ __forceinline__ void red_add_shared(uint32_t saddr, uint32_t v) {
 #define ES_LB_MINB 1
 #endif
 
+// First F entries of an 8-entry residue row (two 16-byte loads at most).
+template <int F>
+__device__ __forceinline__ void row8(const uint4* row, uint32_t (&v)[8]) {
+    if (F > 0) {
+        const uint4 a = row[0];
+        v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+    }
+    if (F > 4) {
+        const uint4 b = row[1];
+        v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+    }
+}
+
 // Everything the cascade tail and the emit need for one item, passed by value into the
 // force-inlined helpers below (nothing escapes to local memory).
 struct TailCtx {
@@ -268,7 +281,7 @@ __device__ __forceinline__ void push(const TailCtx& C, EsQueue* Q, uint32_t lane
 // Warp-uniform: scan one warp-unit w of `item`, whose plan is staged in smem / si.
 template <int F, int LAYOUT, bool COUNT, int WT>
 __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, unsigned char* smem,
-                                          const uint32_t* sm_fast, EsQueue* Q, uint32_t* wcnt,
+                                          EsQueue* Q, uint32_t* wcnt,
                                           uint32_t wcnt_saddr, uint32_t lane, unsigned long long w,
                                           const EsItem& item, uint32_t item_id) {
     TailCtx C;
@@ -305,22 +318,27 @@ __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, u
     const uint16_t* sBK = reinterpret_cast<const uint16_t*>(smem + si.o_BK);
     const uint64_t ob = item.o_begin, oe = item.o_end;
     const uint64_t* list = item.list;
-    const uint32_t n_sm = item.n_sm;
-    uint32_t Feff = (uint32_t)F < L.mask_filters ? (uint32_t)F : L.mask_filters;
-    if (Feff > C.nf) Feff = C.nf;
-    if (LAYOUT == ES_LAYOUT_WORDMASK && Feff > si.F_built) Feff = si.F_built;
+    // word-mask: exactly F filters in the inner-ring stage (the host guarantees F <= filters and
+    // F <= tables built); scalar: a runtime count Feff <= F
+    uint32_t Feff = (uint32_t)F;
+    if (LAYOUT != ES_LAYOUT_WORDMASK) {
+        if (Feff > L.mask_filters) Feff = L.mask_filters;
+        if (Feff > C.nf) Feff = C.nf;
+    }
     C.Feff = Feff;
-    uint32_t qf[F], corr[F], moff[F];
+    constexpr int FA = F > 0 ? F : 1;   // array extent
+    uint32_t qf[FA], corr[FA];
+    const uint32_t* tab[FA];
 #pragma unroll
     for (int f = 0; f < F; ++f) {
         const bool on = (uint32_t)f < Feff;
         qf[f] = on ? C.sFC[f].q : 1u;
         corr[f] = on ? C.sFC[f].corr : 0u;
-        moff[f] = LAYOUT == ES_LAYOUT_WORDMASK ? si.mask_off[f] : (on ? C.sFC[f].off : 0u);
+        tab[f] = LAYOUT == ES_LAYOUT_WORDMASK ? masks_g + si.mask_off[f] : C.allowed_g + (on ? C.sFC[f].off : 0u);
     }
-    uint32_t cnt[F];
+    uint32_t cnt[FA];
 #pragma unroll
-    for (int f = 0; f < F; ++f) cnt[f] = 0u;
+    for (int f = 0; f < FA; ++f) cnt[f] = 0u;
     uint32_t qhead = 0, qsize = 0;
 
     const uint64_t rel = (w - item.unit_begin) * 32ull * L.strip + (uint64_t)lane * L.strip;
@@ -336,9 +354,9 @@ __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, u
     }
     U4 b2{0u, 0u, 0u, 0u};
     uint32_t d2 = 0;
-    uint32_t BQ2[F];
+    uint32_t BQ2[FA];
 #pragma unroll
-    for (int f = 0; f < F; ++f) BQ2[f] = 0u;
+    for (int f = 0; f < FA; ++f) BQ2[f] = 0u;
     bool have = false;
     uint64_t prev_c = 0;
     // every lane runs L.strip steps so the warp-wide votes below see 32 lanes
@@ -365,15 +383,10 @@ __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, u
             if (have && c == prev_c + 1 && d2 + 1u < r2) {
                 uint32_t wm;
                 b2 = addmod(b2, u4(sD2[d2]), M, wm);
+                uint32_t dq[8];
+                row8<F>(sDQ2 + d2 * (ES_FMAX / 4), dq);
 #pragma unroll
-                for (int g = 0; g < F; g += 4) {
-                    const uint4 dq = sDQ2[d2 * (ES_FMAX / 4) + (g >> 2)];
-#pragma unroll
-                    for (int h = 0; h < 4 && g + h < F; ++h) {
-                        const uint32_t dv = h == 0 ? dq.x : (h == 1 ? dq.y : (h == 2 ? dq.z : dq.w));
-                        BQ2[g + h] = red2(BQ2[g + h] + dv + (corr[g + h] & wm), qf[g + h]);
-                    }
-                }
+                for (int f = 0; f < F; ++f) BQ2[f] = red2(BQ2[f] + dq[f] + (corr[f] & wm), qf[f]);
                 ++d2;
             } else if (!(have && c == prev_c)) {
                 b2 = decode_cycle(si, c, M, d2);
@@ -391,7 +404,8 @@ __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, u
             const bool act = (d1 >= lo1) && (d1 < hi1);
             uint32_t wm1;
             const U4 b = addmod(b2, u4(sT1[d1]), M, wm1);
-            const uint32_t* tq_row = reinterpret_cast<const uint32_t*>(sTQ1 + d1 * (ES_FMAX / 4));
+            uint32_t tq[8];
+            row8<F>(sTQ1 + d1 * (ES_FMAX / 4), tq);
             // carry split: sorted slots [split, r0) wrap past M (sentinels at r0)
             uint32_t brw;
             const U4 thr = sub128(M, b, brw);
@@ -412,41 +426,36 @@ __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, u
                 const uint32_t base = wd << 5;
                 const uint32_t cm = split <= base ? valid
                                   : (split >= base + 32u ? 0u : ((0xffffffffu << (split - base)) & valid));
-                bool alive = true;   // warp-uniform: some lane still has a live candidate
+                if (LAYOUT == ES_LAYOUT_WORDMASK) {
+                    // straight-line cascade: two table loads per filter per 32 candidates
 #pragma unroll
-                for (int f = 0; f < F; ++f) {
-                    if (alive && (uint32_t)f < Feff) {
-                        // n mod q_f for the ring-0 base of this outer index
-                        const uint32_t bqf = red2(BQ2[f] + tq_row[f] + (corr[f] & wm1), qf[f]);
-                        if (LAYOUT == ES_LAYOUT_WORDMASK) {
-                            const uint32_t x0 = bqf;
-                            const uint32_t x1 = red1(x0 + corr[f], qf[f]);
-                            uint32_t m0, m1;
-                            if ((uint32_t)f < n_sm) {
-                                const uint32_t* tab = sm_fast + moff[f] + wd;
-                                m0 = tab[x0 * Wn];
-                                m1 = tab[x1 * Wn];
-                            } else {
-                                const uint32_t* tab = masks_g + moff[f] + wd;
-                                m0 = __ldg(tab + x0 * Wn);
-                                m1 = __ldg(tab + x1 * Wn);
-                            }
-                            bits &= (m0 & ~cm) | (m1 & cm);
-                        } else {
+                    for (int f = 0; f < F; ++f) {
+                        const uint32_t x0 = red2(BQ2[f] + tq[f] + (corr[f] & wm1), qf[f]);   // n mod q_f, ring-0 base
+                        const uint32_t x1 = red1(x0 + corr[f], qf[f]);                      // the same after a wrap
+                        const uint32_t m0 = __ldg(tab[f] + x0 * Wn + wd);
+                        const uint32_t m1 = __ldg(tab[f] + x1 * Wn + wd);
+                        bits &= (m0 & ~cm) | (m1 & cm);
+                        if (COUNT) cnt[f] += __popc(bits);
+                    }
+                } else {
+                    bool alive = true;   // warp-uniform: some lane still has a live candidate
+#pragma unroll
+                    for (int f = 0; f < F; ++f) {
+                        if (alive && (uint32_t)f < Feff) {
+                            const uint32_t bqf = red2(BQ2[f] + tq[f] + (corr[f] & wm1), qf[f]);
                             uint32_t nb = 0u, live_bits = bits;
                             while (live_bits) {
                                 const uint32_t i = __ffs(live_bits) - 1u;
                                 live_bits &= live_bits - 1u;
                                 const uint32_t slot = base + i;
                                 const uint32_t m = red2(bqf + sQ0[f * r0 + slot] + ((slot >= split) ? corr[f] : 0u), qf[f]);
-                                const uint32_t wv = ((uint32_t)f < n_sm) ? sm_fast[moff[f] + (m >> 5)]
-                                                                         : __ldg(C.allowed_g + moff[f] + (m >> 5));
+                                const uint32_t wv = __ldg(tab[f] + (m >> 5));
                                 nb |= ((wv >> (m & 31u)) & 1u) << i;
                             }
                             bits = nb;
+                            if (COUNT) cnt[f] += __popc(bits);
+                            if (f + 1 < F && (uint32_t)(f + 1) < Feff) alive = __ballot_sync(0xffffffffu, bits != 0u) != 0u;
                         }
-                        if (COUNT) cnt[f] += __popc(bits);
-                        if (f + 1 < F && (uint32_t)(f + 1) < Feff) alive = __ballot_sync(0xffffffffu, bits != 0u) != 0u;
                     }
                 }
                 // ---- queue the survivors of the inner-ring stage -----------------------------
@@ -462,7 +471,7 @@ __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, u
 #pragma unroll
         for (int f = 0; f < F; ++f) {
             const uint32_t v = __reduce_add_sync(0xffffffffu, cnt[f]);
-            if (lane == 0 && v && gc) atomicAdd(gc + f, (unsigned long long)v);
+            if (lane == 0 && v && gc && (uint32_t)f < Feff) atomicAdd(gc + f, (unsigned long long)v);
         }
         __syncwarp();
         for (uint32_t f = Feff + lane; f < C.nf; f += 32u) {
@@ -497,7 +506,6 @@ __global__ void __launch_bounds__(ES_LB_THREADS, ES_LB_MINB) es_scan_kernel(cons
     const uint32_t tid = threadIdx.x;
     const uint32_t lane = tid & 31u;
     const uint32_t warp = tid >> 5;
-    uint32_t* sm_fast = reinterpret_cast<uint32_t*>(smem + L.fast_off);
     EsQueue* Q = reinterpret_cast<EsQueue*>(smem + L.queue_off) + warp;
     uint32_t* wcnt = reinterpret_cast<uint32_t*>(smem + L.cnt_off) + warp * L.nf_max;
     const uint32_t wcnt_saddr = (uint32_t)__cvta_generic_to_shared(wcnt);
@@ -512,9 +520,6 @@ __global__ void __launch_bounds__(ES_LB_THREADS, ES_LB_MINB) es_scan_kernel(cons
         if (tid == 0) si = *items[0].inst;
         __syncthreads();
         copy_words(reinterpret_cast<uint32_t*>(smem), reinterpret_cast<const uint32_t*>(si.small), si.small_bytes >> 2);
-        if (items[0].sm_fast_words)
-            copy_words(const_cast<uint32_t*>(sm_fast), LAYOUT == ES_LAYOUT_WORDMASK ? si.masks : si.allowed,
-                       items[0].sm_fast_words);
         __syncthreads();
         for (;;) {
             unsigned long long w = 0;
@@ -541,7 +546,7 @@ __global__ void __launch_bounds__(ES_LB_THREADS, ES_LB_MINB) es_scan_kernel(cons
             it_id = __shfl_sync(0xffffffffu, it_id, 0);
             skip = __shfl_sync(0xffffffffu, skip, 0);
             if (skip) continue;
-            scan_unit<F, LAYOUT, COUNT, WT>(L, si, smem, sm_fast, Q, wcnt, wcnt_saddr, lane, w, items[it_id], it_id);
+            scan_unit<F, LAYOUT, COUNT, WT>(L, si, smem, Q, wcnt, wcnt_saddr, lane, w, items[it_id], it_id);
         }
         return;
     }
@@ -595,9 +600,6 @@ __global__ void __launch_bounds__(ES_LB_THREADS, ES_LB_MINB) es_scan_kernel(cons
                     __syncthreads();
                     copy_words(reinterpret_cast<uint32_t*>(smem), reinterpret_cast<const uint32_t*>(si.small),
                                si.small_bytes >> 2);
-                    if (item.sm_fast_words)
-                        copy_words(const_cast<uint32_t*>(sm_fast), LAYOUT == ES_LAYOUT_WORDMASK ? si.masks : si.allowed,
-                                   item.sm_fast_words);
                     __syncthreads();
                     cur_inst = item.inst_id;
                 }
@@ -606,7 +608,7 @@ __global__ void __launch_bounds__(ES_LB_THREADS, ES_LB_MINB) es_scan_kernel(cons
                     if (lane == 0) w = atomicAdd(&s_next, 1ull);
                     w = __shfl_sync(0xffffffffu, w, 0);
                     if (w >= end) break;
-                    scan_unit<F, LAYOUT, COUNT, WT>(L, si, smem, sm_fast, Q, wcnt, wcnt_saddr, lane, w, item, item_id);
+                    scan_unit<F, LAYOUT, COUNT, WT>(L, si, smem, Q, wcnt, wcnt_saddr, lane, w, item, item_id);
                 }
             }
             __syncthreads();
@@ -697,20 +699,33 @@ __global__ void __launch_bounds__(256) es_int_peak_kernel(unsigned long long* si
 
 typedef void (*ScanFn)(const EsLaunch);
 
-template <int LAYOUT, bool COUNT, int WT>
-ScanFn pick_f(uint32_t f) {
-    if (f <= 2) return es_scan_kernel<2, LAYOUT, COUNT, WT>;
-    if (f <= 4) return es_scan_kernel<4, LAYOUT, COUNT, WT>;
-    if (f <= 6) return es_scan_kernel<6, LAYOUT, COUNT, WT>;
-    return es_scan_kernel<8, LAYOUT, COUNT, WT>;
+template <bool COUNT, int WT>
+ScanFn pick_wm(uint32_t f) {
+    switch (f) {
+        case 0: return es_scan_kernel<0, ES_LAYOUT_WORDMASK, COUNT, WT>;
+        case 1: return es_scan_kernel<1, ES_LAYOUT_WORDMASK, COUNT, WT>;
+        case 2: return es_scan_kernel<2, ES_LAYOUT_WORDMASK, COUNT, WT>;
+        case 3: return es_scan_kernel<3, ES_LAYOUT_WORDMASK, COUNT, WT>;
+        case 4: return es_scan_kernel<4, ES_LAYOUT_WORDMASK, COUNT, WT>;
+        case 5: return es_scan_kernel<5, ES_LAYOUT_WORDMASK, COUNT, WT>;
+        case 6: return es_scan_kernel<6, ES_LAYOUT_WORDMASK, COUNT, WT>;
+        default: return es_scan_kernel<8, ES_LAYOUT_WORDMASK, COUNT, WT>;
+    }
+}
+
+template <bool COUNT>
+ScanFn pick_sc(uint32_t f) {
+    if (f <= 2) return es_scan_kernel<2, ES_LAYOUT_SCALAR, COUNT, 0>;
+    if (f <= 4) return es_scan_kernel<4, ES_LAYOUT_SCALAR, COUNT, 0>;
+    return es_scan_kernel<8, ES_LAYOUT_SCALAR, COUNT, 0>;
 }
 
 template <bool COUNT>
 ScanFn pick_w(int layout, uint32_t words, uint32_t f) {
-    if (layout == ES_LAYOUT_SCALAR) return pick_f<ES_LAYOUT_SCALAR, COUNT, 0>(f);
-    if (words == 1) return pick_f<ES_LAYOUT_WORDMASK, COUNT, 1>(f);
-    if (words == 2) return pick_f<ES_LAYOUT_WORDMASK, COUNT, 2>(f);
-    return pick_f<ES_LAYOUT_WORDMASK, COUNT, 0>(f);
+    if (layout == ES_LAYOUT_SCALAR) return pick_sc<COUNT>(f);
+    if (words == 1) return pick_wm<COUNT, 1>(f);
+    if (words == 2) return pick_wm<COUNT, 2>(f);
+    return pick_wm<COUNT, 0>(f);
 }
 
 ScanFn pick(int layout, int count, uint32_t words, uint32_t f) {
@@ -721,7 +736,7 @@ ScanFn pick(int layout, int count, uint32_t words, uint32_t f) {
 
 // Raise the dynamic shared-memory limit of every scan instance once per process/device.
 int es_scan_prepare(int smem_optin_bytes) {
-    const uint32_t fs[4] = {2, 4, 6, 8};
+    const uint32_t fs[8] = {0, 1, 2, 3, 4, 5, 6, 8};
     const uint32_t ws[3] = {1, 2, 3};
     for (int layout = 0; layout < 2; ++layout)
         for (int count = 0; count < 2; ++count)
