@@ -8,6 +8,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -973,3 +974,132 @@ int es_int_peak(double* ops_per_s, double* ms_out) {
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------------------------------
+// es_search_blocks_static: the one entry point that allocates nothing.
+//
+// Some callers cannot call cudaMalloc at all: code running under an external memory manager
+// (a framework that owns every device allocation, a pool with a hard budget), or a service
+// that must not allocate after start-up.  For them this is a variant of the block-ordered
+// multi-block search launch: blocks t0 .. t0+n_blocks-1 of an existing context, scanned in
+// one persistent launch, the first block holding a good survivor ending the search.  The
+// caller passes the inputs (the context's plan tables, built earlier) and the outputs (a
+// survivor buffer, its count and the 4-word minimum).  The launch's scratch -- work counter,
+// search flag, per-block item descriptors and block constants -- lives in the file-scope
+// array below, of fixed size ES_STATIC_MAX_BLOCKS blocks x ES_MAX_FILTERS filters (about
+// 57 KB); every GPU that loads this library keeps it until the process exits.
+namespace {
+
+constexpr size_t kStaticItemsOff = 256;
+constexpr size_t kStaticTconstOff = kStaticItemsOff + sizeof(EsItem) * ES_STATIC_MAX_BLOCKS;
+constexpr size_t kStaticBytes = kStaticTconstOff + 4ull * ES_STATIC_MAX_BLOCKS * ES_MAX_FILTERS;
+
+// [0,8) work counter, [8,16) least block with a good survivor, items, per-block constants
+static __device__ __align__(256) unsigned char g_static_scratch[kStaticBytes];
+
+// Host side: the device address of g_static_scratch per device (the host symbol itself is
+// only a stand-in and must never be passed to a kernel), and a host staging area for the
+// descriptors (static storage: no heap allocation on the call path).
+constexpr int kMaxDevices = 64;
+unsigned char* g_static_ptr[kMaxDevices] = {nullptr};
+EsItem g_static_items[ES_STATIC_MAX_BLOCKS];
+uint32_t g_static_tconst[ES_STATIC_MAX_BLOCKS * ES_MAX_FILTERS];
+std::mutex g_static_mu;
+
+}  // namespace
+
+extern "C" int es_search_blocks_static(const es_ctx* c, uint64_t t0, uint32_t n_blocks,
+                                       es_survivor* d_out, uint64_t out_cap,
+                                       unsigned long long* d_count, unsigned long long* d_min,
+                                       void* stream) {
+    if (!c || !d_out || !d_count || !d_min || out_cap == 0)
+        return fail(ES_ERR_ARG, "null context/output or zero output capacity");
+    if (n_blocks == 0 || n_blocks > ES_STATIC_MAX_BLOCKS)
+        return fail(ES_ERR_RANGE, "n_blocks must be in [1, " + std::to_string(ES_STATIC_MAX_BLOCKS) +
+                                      "] for the static-scratch search");
+    if (t0 > UINT64_MAX - n_blocks) return fail(ES_ERR_RANGE, "block range overflows");
+    const EsInst& I = c->h_inst;
+    if (I.n_filters > ES_MAX_FILTERS) return fail(ES_ERR_RANGE, "too many filters");
+    int dev = 0;
+    ES_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
+    if (dev < 0 || dev >= kMaxDevices) return fail(ES_ERR_RANGE, "device index out of range");
+    std::lock_guard<std::mutex> lock(g_static_mu);
+    if (!g_static_ptr[dev]) {
+        // once per device, with that device current: the scratch array's device address
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(static scratch)");
+        g_static_ptr[dev] = static_cast<unsigned char*>(p);
+    }
+    unsigned char* base = g_static_ptr[dev];
+    unsigned long long* d_unit = reinterpret_cast<unsigned long long*>(base);
+    unsigned long long* d_found = d_unit + 1;
+    EsItem* d_items = reinterpret_cast<EsItem*>(base + kStaticItemsOff);
+    uint32_t* d_tc = reinterpret_cast<uint32_t*>(base + kStaticTconstOff);
+    cudaStream_t st = (cudaStream_t)stream;
+
+    const es_tune& tn = c->tune;
+    const uint32_t nf = I.n_filters;
+    const uint32_t F = stage_filters(tn.layout, tn.mask_filters, nf, I.F_built);
+    const SmemPlan sp = plan_smem((uint32_t)I.small_bytes, nf, tn, 0);
+    const uint64_t per_unit = 32ull * tn.strip;
+    uint64_t cbeg = 0;
+    const uint64_t ncyc = cycles_of(I, 0, I.n_outer, &cbeg);
+    const uint64_t nu = (ncyc + per_unit - 1) / per_unit;
+    for (uint32_t i = 0; i < n_blocks; ++i) {
+        const uint64_t t = t0 + i;
+        EsItem& it = g_static_items[i];
+        memset(&it, 0, sizeof(it));
+        it.inst = c->d_inst;
+        it.tconst = d_tc + (size_t)i * ES_MAX_FILTERS;
+        it.t = t;
+        it.o_begin = 0;
+        it.o_end = I.n_outer;
+        it.c_begin = cbeg;
+        it.c_end = cbeg + ncyc;
+        it.unit_begin = nu * i;
+        it.n_units = nu;
+        for (uint32_t f = 0; f < nf; ++f) {
+            const uint64_t q = c->q[f];
+            g_static_tconst[(size_t)i * ES_MAX_FILTERS + f] = (uint32_t)((t % q) * (uint64_t)(c->M % q) % q);
+        }
+    }
+    ES_CUDA(cudaMemcpyAsync(d_items, g_static_items, sizeof(EsItem) * n_blocks, cudaMemcpyHostToDevice, st),
+            "copy items");
+    ES_CUDA(cudaMemcpyAsync(d_tc, g_static_tconst, 4ull * ES_MAX_FILTERS * n_blocks, cudaMemcpyHostToDevice, st),
+            "copy block constants");
+    ES_CUDA(cudaMemsetAsync(d_unit, 0, 8, st), "memset");
+    ES_CUDA(cudaMemsetAsync(d_found, 0xff, 8, st), "memset");
+    ES_CUDA(cudaMemsetAsync(d_count, 0, 8, st), "memset");
+
+    EsLaunch L;
+    memset(&L, 0, sizeof(L));
+    L.items = d_items;
+    L.n_items = n_blocks;
+    L.threads = tn.threads;
+    L.strip = tn.strip;
+    L.mask_filters = F;
+    L.total_units = nu * n_blocks;
+    L.chunk_max = 16u * (tn.threads / 32u);
+    L.nf_max = std::max<uint32_t>(nf, 1);
+    L.direct = 1;
+    L.unit_counter = d_unit;
+    L.surv = d_out;
+    L.surv_n = d_count;
+    L.surv_cap = out_cap;
+    L.group_found = d_found;
+    L.smem_bytes = sp.bytes;
+    L.tconst_off = sp.tconst_off;
+    L.fast_off = sp.fast_off;
+    L.cnt_off = sp.cnt_off;
+    L.queue_off = sp.queue_off;
+    if (L.total_units) {
+        int grid = 0;
+        if (int e = grid_for(tn.layout, 0, I.W, F, tn, sp.bytes, L.total_units, &grid)) return e;
+        int e = es_launch_scan(L, (int)tn.layout, 0, I.W, grid, st);
+        if (e) return cuda_fail((cudaError_t)e, "scan launch");
+    }
+    int e = es_launch_min(d_out, d_count, out_cap, d_items, 1, d_min, st);
+    if (e) return cuda_fail((cudaError_t)e, "min launch");
+    return ES_OK;
+}

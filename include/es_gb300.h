@@ -164,8 +164,24 @@ int es_batch_group_min(es_batch* b, uint32_t group, int* found, uint64_t* t, uin
                        uint64_t* s_hi);
 int es_batch_item_counts(es_batch* b, uint32_t item, uint64_t* counts, uint32_t n_filters);
 int es_batch_survivors(es_batch* b, es_survivor* out, uint64_t cap, uint64_t* n);
-/* Units claimed per item in the last run (units of skipped blocks included), for tests. */
 int es_batch_destroy(es_batch* b);
+
+/* ---- no-allocation search ---------------------------------------------------------------------
+ * No counterpart in the reference.  For callers that cannot call cudaMalloc (code whose device
+ * memory is owned by another framework or a fixed-budget pool, or that must not allocate after
+ * start-up): blocks t0 .. t0+n_blocks-1 of an existing context scanned as one block-ordered
+ * search in one persistent launch on `stream`, allocating nothing.  The caller passes the outputs:
+ * d_out (out_cap survivor records), d_count (1 word, zeroed by the call) and d_min (4 words:
+ * found, t, s_lo, s_hi of the least n = t*M + s > k+1).  Scratch lives in a file-scope device
+ * array sized for ES_STATIC_MAX_BLOCKS blocks (about 57 KB, held by every GPU that loads the
+ * library until exit); larger n_blocks is rejected with ES_ERR_RANGE.  Stage counts are not
+ * accumulated.  The first call on a device looks up the scratch array's device address: make
+ * it before any stream capture.  Every call shares the one scratch array, so calls that
+ * overlap on the GPU race.  Asynchronous: synchronise `stream` before reading the outputs. */
+#define ES_STATIC_MAX_BLOCKS 64
+int es_search_blocks_static(const es_ctx* ctx, uint64_t t0, uint32_t n_blocks, es_survivor* d_out,
+                            uint64_t out_cap, unsigned long long* d_count, unsigned long long* d_min,
+                            void* stream);
 
 /* ---- measurement -------------------------------------------------------------------------- */
 /* Integer-pipe peak microbenchmark: int32 operations per second of a dependent-free mix of
