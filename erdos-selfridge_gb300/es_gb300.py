@@ -75,6 +75,37 @@ def _tune_from(tun: dict) -> N.Tune:
                        count_stages=int(tun.get("count_stages", 0)))
 
 
+def block_from_tconst(rest_q, rest_Mmodq, tc) -> int:
+    """Recover the block t from its constants tconst_j = (t*M) mod q_j (harness/run_k.py:102-104).
+
+    The reference drivers upload only tconst; the engine also wants t (for the survivor records
+    and the good/n > k+1 test).  t mod q_j is known wherever M is invertible mod q_j, and CRT
+    over pairwise-coprime such q_j gives t modulo their product: exact for every block index
+    below that product (> 2^64 for any plan with a few non-wheel primes)."""
+    t_mod, mod = 0, 1
+    for j, q in enumerate(rest_q):
+        m = rest_Mmodq[j]
+        if math.gcd(m, q) != 1 or math.gcd(mod, q) != 1:
+            continue
+        r = (int(tc[j]) * pow(m, -1, q)) % q
+        k = ((r - t_mod) * pow(mod, -1, q)) % q
+        t_mod += mod * k
+        mod *= q
+        if mod > (1 << 64):
+            break
+    return t_mod
+
+
+def verdict(plan, t: int, surv) -> tuple[list[int], list[int], list[int]]:
+    """Host re-verification of a block's kernel survivors (sieve/gpu_sieve_v9.py:551-557):
+    (all survivors as n, sorted; the good ones; those with n > k+1 that the exact test rejects)."""
+    cands = sorted(plan.idx_to_n(int(i), t) for i in surv)
+    good = [n for n in cands if is_admissible(n, plan.k)]
+    gs = set(good)
+    bad = [n for n in cands if n > plan.k + 1 and n not in gs]
+    return cands, good, bad
+
+
 class _Tconst:
     """Stand-in for the CuPy tconst array: ``.set(host_array)`` uploads block constants."""
 
@@ -154,26 +185,7 @@ class GpuSieve:
 
     # ---------------------------------------------------------------- device plumbing
     def _block_from_tconst(self, tc: np.ndarray) -> int:
-        """Recover t from tconst when the caller only uploads constants (run_k.py path).
-
-        tconst_j = t*M mod q_j, so t mod q_j is known wherever M is invertible mod q_j; CRT over
-        those filters gives t modulo their product, exact for every practical block index."""
-        t_mod, mod = 0, 1
-        for j, q in enumerate(self.rest_q):
-            m = self.rest_Mmodq[j]
-            if math.gcd(m, q) != 1:
-                continue
-            r = (int(tc[j]) * pow(m, -1, q)) % q
-            g = math.gcd(mod, q)
-            if g != 1:
-                continue
-            # combine t = t_mod (mod mod) with t = r (mod q)
-            k = ((r - t_mod) * pow(mod, -1, q)) % q
-            t_mod += mod * k
-            mod *= q
-            if mod > (1 << 64):
-                break
-        return t_mod
+        return block_from_tconst(self.rest_q, self.rest_Mmodq, tc)
 
     def _set_tconst(self, tc: np.ndarray) -> None:
         tc = np.ascontiguousarray(tc[:max(self.nrest, 1)], dtype=np.uint32)
@@ -220,12 +232,8 @@ class GpuSieve:
             ostart += ocount
         return survivors
 
-    def _verdict(self, t: int, surv: list[int], t0: float):
-        P = self.plan
-        cands = sorted(P.idx_to_n(i, t) for i in surv)
-        good = [n for n in cands if is_admissible(n, P.k)]
-        bad = [n for n in cands if n > P.k + 1 and n not in good]
-        return cands, good, bad
+    def _verdict(self, t: int, surv: list[int]):
+        return verdict(self.plan, t, surv)
 
     def search(self, max_blocks: int | None = None, log=None) -> dict:
         """Blocks t = 0, 1, ... until the first block holding a good survivor.
@@ -256,7 +264,7 @@ class GpuSieve:
                 found_t = found
                 self.residues_checked += (found_t - t) * P.R
                 surv = self.scan_block(found_t)
-            cands, good, bad = self._verdict(found_t, surv, t0)
+            cands, good, bad = self._verdict(found_t, surv)
             if bad:
                 return {"k": P.k, "status": "DISAGREEMENT", "kernel_survivors": cands[:20],
                         "ref_rejected": bad[:20], "block": found_t, "wall": time.time() - t0}

@@ -1,0 +1,96 @@
+"""CPU model of the scan kernel's arithmetic (test infrastructure).
+
+Re-derives, in plain Python integers, every table the device uses (sorted inner ring, 32-bit
+carry-split keys and buckets, ring-1 residues, word-mask phases, wrap corrections) and walks
+positions exactly the way es_scan_kernel does: b2 from rings >= 2, one ring-1 term, the carry
+split of the inner ring, the word-mask stage over the first F filters, then the exact tail.
+It isolates "the decomposition is wrong" from "the CUDA is wrong", like the reference's CPU
+emulation of its kernel index scheme (tests/test_enumeration.py).
+"""
+from __future__ import annotations
+
+
+class KernelModel:
+    def __init__(self, plan, F: int = 4):
+        M = plan.M
+        self.k, self.M = plan.k, M
+        terms = [[(a * b) % M for a in res] for (_, res), b in zip(plan.rings, plan.basis)]
+        while len(terms) < 3:
+            terms.append([0])
+        self.terms = terms
+        self.r0, self.r1, self.r2 = len(terms[0]), len(terms[1]), len(terms[2])
+        self.radix = [len(t) for t in terms]
+        order = sorted(range(self.r0), key=lambda i: terms[0][i])
+        self.S0 = [terms[0][i] for i in order]
+        self.I0 = order
+        bl = M.bit_length()
+        self.sh = bl - 32 if bl > 32 else 0
+        self.K0 = [v >> self.sh for v in self.S0] + [0xFFFFFFFF]      # sentinel
+        kb = (M >> self.sh).bit_length()
+        self.bsh = kb - 10 if kb > 10 else 0
+        self.BK = [sum(1 for x in self.K0[:-1] if x < (b << self.bsh)) for b in range(1025)]
+        self.q = [plan.info[p][0] for p in plan.rest]
+        self.ok = [set(plan.info[p][1]) for p in plan.rest]
+        self.corr = [(q - M % q) % q for q in self.q]
+        self.F = min(F, len(self.q))
+        self.W = (self.r0 + 31) // 32
+
+    def split(self, b: int) -> int:
+        """Sorted slots [split, r0) wrap past M: the kernel's key + bucket search."""
+        thr = self.M - b
+        t32 = thr >> self.sh
+        s = self.BK[t32 >> self.bsh]
+        while self.K0[s] < t32:
+            s += 1
+        while self.K0[s] == t32 and s < self.r0 and self.S0[s] < thr:
+            s += 1
+        return s
+
+    def b2(self, c: int) -> int:
+        rem, acc = c, 0
+        for j in range(2, len(self.terms)):
+            rem, d = divmod(rem, self.radix[j])
+            acc = (acc + self.terms[j][d]) % self.M
+        return acc
+
+    def scan(self, t: int, outer) -> tuple[list[int], list[int]]:
+        M, r0 = self.M, self.r0
+        nf = len(self.q)
+        tc = [((t % q) * (M % q)) % q for q in self.q]
+        counts = [0] * nf
+        surv = []
+        for oidx in outer:
+            c, d1 = divmod(int(oidx), self.r1)
+            b2 = self.b2(c)
+            BQ2 = [(b2 % q + tc[f]) % q for f, q in enumerate(self.q[:self.F])]
+            s1 = b2 + self.terms[1][d1]
+            w1 = s1 >= M
+            b = s1 - M if w1 else s1
+            sp = self.split(b)
+            assert sp == sum(1 for v in self.S0 if v + b < M), "carry split"
+            for wd in range(self.W):
+                n_here = min(32, r0 - 32 * wd)
+                bits = (1 << n_here) - 1
+                cm = sum(1 << i for i in range(n_here) if 32 * wd + i >= sp)
+                for f in range(self.F):
+                    q = self.q[f]
+                    x0 = (BQ2[f] + self.terms[1][d1] % q + (self.corr[f] if w1 else 0)) % q
+                    x1 = (x0 + self.corr[f]) % q
+                    m0 = sum(1 << i for i in range(n_here) if (x0 + self.S0[32 * wd + i]) % q in self.ok[f])
+                    m1 = sum(1 << i for i in range(n_here) if (x1 + self.S0[32 * wd + i]) % q in self.ok[f])
+                    bits &= (m0 & ~cm) | (m1 & cm)
+                    counts[f] += bin(bits).count("1")
+                for i in range(n_here):
+                    if not (bits >> i) & 1:
+                        continue
+                    slot = 32 * wd + i
+                    s = (b + self.S0[slot]) % M
+                    ok = True
+                    for f in range(self.F, nf):
+                        if (s % self.q[f] + tc[f]) % self.q[f] not in self.ok[f]:
+                            ok = False
+                            break
+                        counts[f] += 1
+                    if ok:
+                        surv.append(int(oidx) * r0 + self.I0[slot])
+        return sorted(surv), counts

@@ -1,0 +1,129 @@
+"""CPU: host logic of the drop-in engine, with the device replaced by a fake backed by the C
+oracle (block loop, block-ordered search, DISAGREEMENT on a planted fault, overflow fallback)."""
+import numpy as np
+import pytest
+
+
+class FakeCtx:
+    """Stands in for es_native.Context; scans with the CPU oracle."""
+
+    def __init__(self, plan, capacity=1 << 20, plant=None):
+        import es_oracle as O
+        self.plan, self.capacity, self.plant = plan, capacity, plant
+        self.T = O.CTables(plan)
+        self.r0 = plan.radix[0] if plan.radix else 1
+        self.n_outer = plan.R // self.r0
+        self.n_filters = len(plan.rest)
+        self.t, self.surv = 0, []
+
+    def set_block(self, t, tconst=None):
+        self.t = int(t)
+
+    def reset(self):
+        self.surv = []
+
+    def launch(self, ostart, ocount):
+        import es_oracle as O
+        s, _, _ = O.scan_c(self.T, self.t, o_range=(ostart, ostart + ocount), threads=2)
+        self.surv.extend(s)
+        if self.plant is not None and ostart == 0:
+            self.surv.append(self.plant)
+
+    def count(self):
+        return len(self.surv)
+
+    def survivors(self):
+        if len(self.surv) > self.capacity:
+            raise RuntimeError("overflow")
+        return np.array(self.surv, dtype=np.uint64)
+
+
+class FakeBatch:
+    """Stands in for es_native.Batch: blocks of one group, least good (t, s)."""
+
+    def __init__(self, ctxs, items, tune=None):
+        self.ctx, self.items = ctxs[0], items
+
+    def run(self, use_graph=False):
+        from es_plan import is_admissible
+        self.best = None
+        for (_, _, t, ob, oe) in self.items:
+            self.ctx.set_block(t)
+            self.ctx.reset()
+            self.ctx.launch(ob, oe - ob)
+            P = self.ctx.plan
+            good = [n for n in (P.idx_to_n(int(i), t) for i in self.ctx.surv) if n > P.k + 1 and is_admissible(n, P.k)]
+            if good:
+                self.best = (t, min(good) - t * P.M)
+                return
+
+    def group_min(self, g):
+        return self.best
+
+    def close(self):
+        pass
+
+
+def _sieve(monkeypatch, k, plant=None, cap=1 << 20, tun=None):
+    import es_gb300
+    plan = es_gb300.Plan(k, tun)
+    fake = FakeCtx(plan, cap, plant)
+    monkeypatch.setattr(es_gb300.N, "Context", lambda p, t, capacity=None: fake)
+    monkeypatch.setattr(es_gb300.N, "Batch", FakeBatch)
+    return es_gb300.GpuSieve(plan), fake
+
+
+@pytest.mark.parametrize("k", [1, 2, 5, 30, 60, 70, 97])
+def test_search_control_flow_matches_bfile(monkeypatch, bfile, k):
+    sieve, _ = _sieve(monkeypatch, k)
+    res = sieve.search(None)
+    assert res["status"] == "FOUND" and res["g"] == bfile[k]
+    assert res["residues_checked"] == (res["block"] + 1) * sieve.plan.R
+
+
+def test_planted_fault_is_a_disagreement(monkeypatch):
+    """A kernel 'survivor' whose n fails the exact test must end the search as DISAGREEMENT."""
+    import es_gb300
+    plan = es_gb300.Plan(120)
+    bad_idx = next(i for i in range(plan.R) if plan.idx_to_n(i, 0) > 121
+                   and not es_gb300.is_admissible(plan.idx_to_n(i, 0), 120))
+    sieve, _ = _sieve(monkeypatch, 120, plant=bad_idx)
+    res = sieve.search(1)
+    assert res["status"] == "DISAGREEMENT"
+    assert plan.idx_to_n(bad_idx, 0) in res["ref_rejected"]
+
+
+def test_exhausted_blocks(monkeypatch):
+    sieve, _ = _sieve(monkeypatch, 30)   # g(30) lies in block 9
+    res = sieve.search(3)
+    assert res["status"] == "EXHAUSTED_BLOCKS" and res["blocks"] == 3
+
+
+def test_overflow_falls_back_then_raises(monkeypatch):
+    sieve, fake = _sieve(monkeypatch, 40, cap=1, tun={"max_survivors": 1, "chunk_log2": 5})
+    with pytest.raises(RuntimeError):
+        sieve.scan_block(0)
+
+
+def test_block_from_tconst_and_verdict():
+    import es_gb300
+    import es_native as N
+    P = es_gb300.Plan(390)
+    rq = [P.info[p][0] for p in P.rest]
+    rm = [P.M % q for q in rq]
+    for t in (0, 3, 99991, 2**50 + 3):
+        assert es_gb300.block_from_tconst(rq, rm, N.tconst_for(P, t)) == t
+    Q = es_gb300.Plan(60)
+    cands, good, bad = es_gb300.verdict(Q, 6, [0, 1, 2])
+    assert cands == sorted(Q.idx_to_n(i, 6) for i in (0, 1, 2))
+    assert set(good) | set(bad) <= set(cands)
+
+
+def test_load_known(tmp_path):
+    import es_gb300
+    a = tmp_path / "a.txt"
+    b = tmp_path / "b.txt"
+    a.write_text("1 3\n2 6\n# comment\n")
+    b.write_text("2 99\n3 7\n")
+    known = es_gb300.load_known(str(a), str(b), str(tmp_path / "missing.txt"))
+    assert known == {1: (3, "a.txt"), 2: (6, "a.txt"), 3: (7, "b.txt")}
