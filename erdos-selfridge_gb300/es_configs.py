@@ -1,0 +1,203 @@
+#!/usr/bin/env python3
+"""Fixed-scope scans of the engine's measurement suite (one GPU), as reusable functions + CLI.
+
+    python erdos-selfridge_gb300/es_configs.py batch64 [--json out.json]
+    python erdos-selfridge_gb300/es_configs.py k390 [--log2-positions 40]
+    python erdos-selfridge_gb300/es_configs.py small-k --bfile data/b003458.txt
+
+* small-k: g(k) for k = 40..120 by the block-ordered search (GpuSieve.search), each checked
+  against known values when a b-file is given.
+* batch64: 64 seeded instances (k uniform in 150..400, range lengths log-uniform in 2^20..2^32
+  positions of block 0, each with its own planner wheel) in ONE persistent work-stealing launch
+  replayed from a CUDA graph, launch shape from the autotuner, against one launch per instance.
+* k390: the two recorded k = 390 wheels (primary and confirmation of evidence/through400/
+  runs.json) over positions [0, 2^40) of block 0 in one persistent launch; every survivor of
+  either wheel that the other wheel's scanned prefix covers must be a survivor there too.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+if HERE not in sys.path:
+    sys.path.insert(0, HERE)
+
+import es_autotune  # noqa: E402
+import es_gb300  # noqa: E402
+import es_native as N  # noqa: E402
+
+# The recorded k = 390 wheels (evidence/through400/runs.json, terms[k=390].primary/.confirmation)
+K390_WHEELS = {
+    "primary": [[3, 6], [2, 9], [211, 1], [139, 1], [103, 1], [137, 1], [101, 1], [67, 1], [5, 2],
+                [199, 1], [23, 2], [79, 1], [197, 1], [131, 1], [7, 2], [17, 1]],
+    "confirmation": [[3, 6], [2, 9], [211, 1], [139, 1], [103, 1], [137, 1], [101, 1], [67, 1],
+                     [199, 1], [23, 2], [11, 1], [79, 1], [197, 1], [131, 1], [7, 2], [17, 1]],
+}
+
+
+def batch64_instances(seed: int = 0, count: int = 64):
+    """(k_i, L_i): k uniform in 150..400, L log-uniform in [2^20, 2^32) positions."""
+    rng = np.random.default_rng(seed)
+    ks = rng.integers(150, 401, size=count)
+    L = np.floor(2.0 ** rng.uniform(20, 32, size=count)).astype(np.int64)
+    return [int(x) for x in ks], [int(x) for x in L]
+
+
+def small_k(ks=range(40, 121), known: dict | None = None) -> dict:
+    t0 = time.time()
+    out = {}
+    for k in ks:
+        r = es_gb300.GpuSieve(es_gb300.Plan(k)).search(None)
+        out[k] = {"status": r["status"], "g": r.get("g"), "block": r.get("block"),
+                  "match": (known.get(k) == r.get("g")) if known else None}
+    return {"cases": out, "wall_s": time.time() - t0,
+            "all_match": all(v["match"] for v in out.values()) if known else None}
+
+
+def batch64(seed: int = 0, autotune: bool = True, reps: int = 5, check_oracle_log2: int = 24) -> dict:
+    ks, L = batch64_instances(seed)
+    plans = [es_gb300.Plan(k) for k in ks]
+    tune0 = N.make_tune(**es_autotune.DEFAULT)
+    ctxs = [N.Context(p, tune0) for p in plans]
+    items, positions = [], 0
+    for i, (p, c, length) in enumerate(zip(plans, ctxs, L)):
+        n_outer = -(-min(length, p.R) // c.r0)
+        items.append((i, i, 0, 0, n_outer))
+        positions += n_outer * c.r0
+    tune, tune_ms = (es_autotune.tune_batch(ctxs, items) if autotune
+                     else (dict(es_autotune.DEFAULT), None))
+    b = N.Batch(ctxs, items, N.make_tune(**tune))
+    b.run(use_graph=True)
+    b.sync()
+    ms = []
+    for _ in range(reps):
+        b.run(use_graph=True)
+        ms.append(b.sync())
+    batch_ms = statistics.median(ms)
+    surv = b.survivors()
+    b.close()
+    # one launch per instance, each on its own context, synchronised like a per-instance driver
+    single_ms, t_wall = [], time.perf_counter()
+    for c, (_, _, _, ob, oe) in zip(ctxs, items):
+        c.set_tune(N.make_tune(**tune))
+        c.set_block(0)
+        c.reset()
+        single_ms.append(c.launch_timed(ob, oe - ob))
+    single_wall = (time.perf_counter() - t_wall) * 1e3
+    # parity: per-item stage counts (counting batch) against the C oracle on the small items
+    checked = mismatched = 0
+    try:
+        sys.path.insert(0, os.path.join(os.path.dirname(HERE), "oracle"))
+        import es_oracle as O
+    except ImportError:
+        O = None
+    if O is not None:
+        bc = N.Batch(ctxs, items, N.make_tune(**dict(tune, count_stages=1)))
+        bc.run(use_graph=False)
+        bc.sync()
+        sc = bc.survivors()
+        for i, (p, c, it) in enumerate(zip(plans, ctxs, items)):
+            if (it[4] - it[3]) * c.r0 > (1 << check_oracle_log2):
+                continue
+            ws, wc, _ = O.scan_c(p, 0, o_range=(it[3], it[4]))
+            got = sorted(int(r["idx"]) for r in sc if r["item"] == i)
+            ok = ws == got and wc == [int(x) for x in bc.item_counts(i)]
+            checked += 1
+            mismatched += 0 if ok else 1
+        bc.close()
+    for c in ctxs:
+        c.close()
+    return {"instances": len(items), "positions": positions, "tune": tune,
+            "batch_ms": batch_ms, "batch_Gcand_s": positions / batch_ms / 1e6,
+            "single_ms_device_sum": sum(single_ms), "single_ms_wall": single_wall,
+            "single_Gcand_s_device": positions / sum(single_ms) / 1e6,
+            "single_Gcand_s_wall": positions / single_wall / 1e6,
+            "speedup_vs_single_wall": single_wall / batch_ms,
+            "survivors": int(len(surv)), "oracle_checked_items": checked,
+            "oracle_mismatches": mismatched}
+
+
+def k390(log2_positions: int = 40, filter_orders: dict | None = None, tune: dict | None = None,
+         reps: int = 1) -> dict:
+    """Both recorded wheels over [0, 2^log2_positions) of block 0 in one persistent launch."""
+    plans = {}
+    for role, wheel in K390_WHEELS.items():
+        order = (filter_orders or {}).get(role)
+        plans[role] = es_gb300.Plan(390, None, wheel, filter_order=order)
+    t = dict(es_autotune.DEFAULT, **(tune or {}))
+    ctxs = [N.Context(plans[r], N.make_tune(**t)) for r in ("primary", "confirmation")]
+    pos = 1 << log2_positions
+    items = []
+    for i, c in enumerate(ctxs):
+        n_outer = min(c.n_outer, -(-pos // c.r0))
+        items.append((i, i, 0, 0, n_outer))
+    b = N.Batch(ctxs, items, N.make_tune(**t))
+    b.run(use_graph=True)
+    ms = [b.sync()]
+    for _ in range(reps - 1):
+        b.run(use_graph=True)
+        ms.append(b.sync())
+    surv = b.survivors()
+    b.close()
+    res = {}
+    sets = {}
+    for i, role in enumerate(("primary", "confirmation")):
+        P = plans[role]
+        idx = sorted(int(r["idx"]) for r in surv if r["item"] == i)
+        sets[role] = (P, set(idx), items[i][4] * ctxs[i].r0)
+        res[role] = {"M_bits": P.M.bit_length(), "r0": P.radix[0], "positions": items[i][4] * ctxs[i].r0,
+                     "survivors": len(idx), "survivors_n": [str(P.idx_to_n(x, 0)) for x in idx[:64]]}
+    # cross-wheel agreement: n admissible, n < M_other and inside the other's scanned prefix
+    disagree = []
+    for a, b_ in (("primary", "confirmation"), ("confirmation", "primary")):
+        PA, SA, _ = sets[a]
+        PB, SB, limB = sets[b_]
+        for ia in SA:
+            n = PA.idx_to_n(ia, 0)
+            if n >= PB.M:
+                continue
+            tb = PB.n_to_idx(n)
+            if tb is None or tb[1] >= limB:
+                continue
+            if tb[1] not in SB:
+                disagree.append({"n": str(n), "in": a, "missing_from": b_})
+    total_pos = sum(v["positions"] for v in res.values())
+    ms_med = statistics.median(ms)
+    for c in ctxs:
+        c.close()
+    return {"wheels": res, "ms": ms_med, "Gcand_s": total_pos / ms_med / 1e6, "tune": t,
+            "cross_checked": True, "disagreements": disagree}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("which", choices=["small-k", "batch64", "k390"])
+    ap.add_argument("--json", default=None)
+    ap.add_argument("--bfile", default=None)
+    ap.add_argument("--log2-positions", type=int, default=40)
+    ap.add_argument("--no-autotune", action="store_true")
+    a = ap.parse_args()
+    if a.which == "small-k":
+        known = {k: g for k, (g, _) in es_gb300.load_known(a.bfile).items()} if a.bfile else None
+        out = small_k(known=known)
+    elif a.which == "batch64":
+        out = batch64(autotune=not a.no_autotune)
+    else:
+        out = k390(a.log2_positions)
+    s = json.dumps(out, default=str)
+    if a.json:
+        with open(a.json, "w") as f:
+            f.write(s + "\n")
+    print(s)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,432 @@
+#!/usr/bin/env python3
+"""Learned planner: an MLP cost model that stands in for the knapsack planner's analytic estimate.
+
+The reference planner (sieve/gpu_sieve_v9.py:187-227) ranks wheels by expected residue checks
+R / (1 - e^{-M/E}) and orders filters by conditional pass rate (v9:230-237); it assumes every plan
+scans at the same rate.  On the GPU the rate is not constant: it depends on the inner radix, on
+whether the first filters' word-mask tables stay in L1, on how fast the first filters reject, on
+the number of rings.  This module
+
+1. enumerates ~40 candidate plans per k: wheels from the reference's own sweep grids
+   (harness/plan_sweep.py:33-49: planner, n_mult, cost_scale, m_cap_bits) and banned-prime
+   re-plans (harness/plan_sweep.py:52-58), each with several filter orders;
+2. probes each on the GPU: 2^28 positions of block 0 -> Gcand/s and per-filter pass fractions;
+3. trains a 3-layer FP32 MLP (64 hidden, ReLU) with this library's own CUDA kernels
+   (es_mlp_*) to predict log throughput and log expected positions to the first survivor;
+4. chooses, per k, the plan with the least predicted time = positions / throughput, and compares
+   it on held-out k with the analytic choice (least expected checks, reference filter order).
+
+The analytic planner stays the fallback (no model, or a k outside the trained range) and the judge
+of the model's error: both predictions are scored against the measured outcome.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import math
+import multiprocessing as mp
+import os
+import statistics
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+if HERE not in sys.path:
+    sys.path.insert(0, HERE)
+
+import es_plan  # noqa: E402
+
+N_FIRST = 6          # filters described individually in the features
+FEATURE_DIM = 14 + 3 * N_FIRST
+PROBE_LOG2 = 28
+
+
+# ------------------------------------------------------------------ the GPU MLP (ctypes)
+class MLP:
+    """3-layer FP32 MLP on the GPU (es_mlp_* kernels): in -> 64 -> 64 -> out, ReLU."""
+
+    def __init__(self, in_dim: int, out_dim: int = 2, hidden: int = 64, seed: int = 0):
+        import es_native as N
+        L = N.lib()
+        f32p, u64 = C.POINTER(C.c_float), C.c_uint64
+        for name, args in (("es_mlp_create", [C.c_uint32, C.c_uint32, C.c_uint32, u64, C.POINTER(C.c_void_p)]),
+                           ("es_mlp_destroy", [C.c_void_p]),
+                           ("es_mlp_num_params", [C.c_void_p, C.POINTER(u64)]),
+                           ("es_mlp_get_params", [C.c_void_p, f32p, u64]),
+                           ("es_mlp_set_params", [C.c_void_p, f32p, u64]),
+                           ("es_mlp_forward", [C.c_void_p, f32p, u64, f32p]),
+                           ("es_mlp_loss_grad", [C.c_void_p, f32p, f32p, u64, f32p, f32p]),
+                           ("es_mlp_train", [C.c_void_p, f32p, f32p, u64, C.c_uint32, C.c_uint32, C.c_float, u64, f32p])):
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = C.c_int
+        L.es_mlp_last_error.restype = C.c_char_p
+        self.L = L
+        self.in_dim, self.out_dim, self.hidden = in_dim, out_dim, hidden
+        h = C.c_void_p()
+        self._check(L.es_mlp_create(in_dim, hidden, out_dim, seed, C.byref(h)))
+        self.h = h
+        n = C.c_uint64()
+        self._check(L.es_mlp_num_params(h, C.byref(n)))
+        self.n_params = n.value
+
+    def _check(self, rc):
+        if rc != 0:
+            raise RuntimeError(f"es_mlp error {rc}: {self.L.es_mlp_last_error().decode()}")
+
+    @staticmethod
+    def _f32(a):
+        return np.ascontiguousarray(a, dtype=np.float32)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.es_mlp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def params(self) -> np.ndarray:
+        out = np.zeros(self.n_params, dtype=np.float32)
+        self._check(self.L.es_mlp_get_params(self.h, out.ctypes.data_as(C.POINTER(C.c_float)), self.n_params))
+        return out
+
+    def set_params(self, p) -> None:
+        p = self._f32(p)
+        self._check(self.L.es_mlp_set_params(self.h, p.ctypes.data_as(C.POINTER(C.c_float)), self.n_params))
+
+    def forward(self, X) -> np.ndarray:
+        X = self._f32(X)
+        Y = np.zeros((X.shape[0], self.out_dim), dtype=np.float32)
+        fp = C.POINTER(C.c_float)
+        self._check(self.L.es_mlp_forward(self.h, X.ctypes.data_as(fp), X.shape[0], Y.ctypes.data_as(fp)))
+        return Y
+
+    def loss_grad(self, X, T) -> tuple[float, np.ndarray]:
+        X, T = self._f32(X), self._f32(T)
+        g = np.zeros(self.n_params, dtype=np.float32)
+        loss = C.c_float()
+        fp = C.POINTER(C.c_float)
+        self._check(self.L.es_mlp_loss_grad(self.h, X.ctypes.data_as(fp), T.ctypes.data_as(fp), X.shape[0],
+                                            C.byref(loss), g.ctypes.data_as(fp)))
+        return loss.value, g
+
+    def train(self, X, T, epochs: int = 400, batch: int = 256, lr: float = 1e-3, seed: int = 0) -> float:
+        X, T = self._f32(X), self._f32(T)
+        loss = C.c_float()
+        fp = C.POINTER(C.c_float)
+        self._check(self.L.es_mlp_train(self.h, X.ctypes.data_as(fp), T.ctypes.data_as(fp), X.shape[0],
+                                        epochs, batch, lr, seed, C.byref(loss)))
+        return loss.value
+
+
+# ------------------------------------------------------------------ features and targets
+def _log2(x: float) -> float:
+    return math.log2(x) if x > 0 else 0.0
+
+
+def features(plan) -> np.ndarray:
+    """Description of a plan (wheel + cascade order) for the cost model."""
+    k = plan.k
+    r0 = plan.radix[0] if plan.radix else 1
+    r1 = plan.radix[1] if len(plan.radix) > 1 else 1
+    W = (r0 + 31) // 32
+    rates = plan.conditional_pass_rates()
+    qs = [plan.info[p][0] for p in plan.rest]
+    log2E = -math.log2(plan.density_all) if plan.density_all > 0 else 0.0
+    first_tab = sum(q * W * 4 for q in qs[:4])
+    f = [k / 400.0, log2E / 128.0, _log2(plan.M) / 128.0, _log2(plan.R) / 64.0, _log2(r0) / 8.0,
+         _log2(r1) / 8.0, len(plan.radix) / 20.0, len(plan.rest) / 80.0, W / 4.0,
+         _log2(first_tab) / 24.0,
+         sum(_log2(r) for r in rates[:4]) / -16.0,
+         sum(_log2(r) for r in rates) / -64.0,
+         _log2(plan._true_cost()) / 64.0,
+         (r0 % 32) / 32.0]
+    for j in range(N_FIRST):
+        if j < len(qs):
+            f += [_log2(qs[j]) / 20.0, rates[j], _log2(qs[j] * W * 4) / 24.0]
+        else:
+            f += [0.0, 1.0, 0.0]
+    assert len(f) == FEATURE_DIM
+    return np.array(f, dtype=np.float32)
+
+
+def expected_positions(plan, counts, n_probe: int, min_count: int = 200) -> float:
+    """Expected positions the block-ordered search scans before it ends: R / (1 - e^{-R p}),
+    p = survivor probability per position from the probe's measured pass fractions (analytic
+    conditional rates where a stage saw fewer than min_count candidates)."""
+    rates = plan.conditional_pass_rates()
+    logp, prev = 0.0, n_probe
+    for j, r in enumerate(rates):
+        c = counts[j] if j < len(counts) else 0
+        if prev >= min_count and c > 0:
+            logp += math.log(c / prev)
+        else:
+            logp += math.log(r)
+        prev = c
+    Rp = plan.R * math.exp(logp)
+    if Rp < 1e-12:
+        return math.exp(-logp)           # 1/p: far fewer than one survivor per block
+    return plan.R / -math.expm1(-Rp)
+
+
+# ------------------------------------------------------------------ candidate plans
+WHEEL_TUNES = [
+    None,                                            # the reference default (truecost)
+    {"planner": "knapsack", "n_mult": 1.0},
+    {"planner": "knapsack", "n_mult": 0.25},
+    {"planner": "knapsack", "n_mult": 4.0},
+    {"m_cap_bits": 100},
+    {"m_cap_bits": 80},
+    {"cost_scale": 64},
+]
+
+
+def _orders(plan, rng) -> list[tuple[str, list[int]]]:
+    ref = list(plan.rest)
+    out = [("reference", ref)]
+    W = ((plan.radix[0] if plan.radix else 1) + 31) // 32
+    rates = dict(zip(ref, plan.conditional_pass_rates()))
+    # table-aware: rejection per unit of word-mask table footprint for the first slots
+    def score(p):
+        q = plan.info[p][0]
+        return (1.0 - rates[p]) / (1.0 + q * W * 4 / 65536.0)
+    head = sorted(ref, key=score, reverse=True)[:N_FIRST]
+    out.append(("table-aware", head + [p for p in ref if p not in head]))
+    small = sorted(ref[:8], key=lambda p: plan.info[p][0])
+    out.append(("small-q-first", small + ref[8:]))
+    for i in range(3):
+        perm = ref[:8]
+        rng.shuffle(perm)
+        out.append((f"shuffle{i}", perm + ref[8:]))
+    seen, uniq = set(), []
+    for name, o in out:
+        key = tuple(o)
+        if key not in seen:
+            seen.add(key)
+            uniq.append((name, o))
+    return uniq
+
+
+def candidate_specs(k: int, seed: int = 0) -> list[dict]:
+    """Candidate (wheel, order) specs for k; deterministic for a seed."""
+    rng = np.random.default_rng(seed * 1000003 + k)
+    specs, wheels = [], set()
+    base = es_plan.Plan(k)
+    log2E = -math.log2(base.density_all)
+    wheel_list = []
+    for tun in WHEEL_TUNES:
+        P = base if tun is None else es_plan.Plan(k, tun)
+        wheel_list.append(("default" if tun is None else json.dumps(tun, sort_keys=True), P))
+    for ban in sorted({p for p, _ in base.wheel})[:2]:
+        ps = [p for p in es_plan.primes_upto(k) if p != ban]
+        w = es_plan.plan_wheel(k, ps, log2E, dict(es_plan.TUNABLES))
+        wheel_list.append((f"ban{ban}", es_plan.Plan(k, None, [[p, T] for p, T in w])))
+    for wname, P in wheel_list:
+        key = tuple(sorted(P.wheel))
+        if key in wheels or not P.wheel:
+            continue
+        wheels.add(key)
+        for oname, order in _orders(P, rng):
+            specs.append({"k": k, "wheel": [[p, T] for p, T in P.wheel], "order": order,
+                          "wheel_name": wname, "order_name": oname})
+    return specs
+
+
+def _materialise(spec) -> dict:
+    """Worker side: build the plan, its device arrays and its analytic description."""
+    import es_native as N
+    P = es_plan.Plan(spec["k"], None, spec["wheel"]).with_order(spec["order"])
+    A = N.PlanArrays(P)
+    return {"spec": spec, "features": features(P), "R": P.R, "M_bits": P.M.bit_length(),
+            "true_cost": P._true_cost(), "rates": P.conditional_pass_rates(),
+            "arrays": (P.k, A.radix, A.term_lo, A.term_hi, A.q, A.allowed, P.M), "r0": P.radix[0],
+            "ref_order": spec["order_name"] == "reference"}
+
+
+def _specs_for(k):
+    return candidate_specs(k)
+
+
+# ------------------------------------------------------------------ GPU probes
+def probe(item: dict, tune=None, log2_pos: int = PROBE_LOG2, reps: int = 3) -> dict:
+    """Time 2^log2_pos positions of block 0 (median of reps) and take stage counts once."""
+    import es_native as N
+    k, radix, lo, hi, q, allowed, M = item["arrays"]
+    A = N.PlanArrays.from_arrays(k, radix, lo, hi, q, allowed, M)
+    t = N.make_tune(**dict(tune or {}, count_stages=1))
+    ctx = N.Context.from_arrays(A, t, len(q))
+    try:
+        r0 = int(radix[0]) if len(radix) and radix[0] else 1
+        n_outer = max(1, min(ctx.n_outer, (1 << log2_pos) // r0))
+        ctx.set_block(0, np.zeros(len(q), dtype=np.uint32))
+        ctx.reset_counts()
+        ctx.reset()
+        ctx.launch(0, n_outer)
+        counts = [int(x) for x in ctx.stage_counts()]
+        ctx.set_tune(N.make_tune(**dict(tune or {}, count_stages=0)))
+        ctx.reset()
+        ctx.launch_timed(0, n_outer)
+        ms = []
+        for _ in range(reps):
+            ctx.reset()
+            ms.append(ctx.launch_timed(0, n_outer))
+        m = statistics.median(ms)
+    finally:
+        ctx.close()
+    n_pos = n_outer * r0
+    return {"gcand": n_pos / m / 1e6, "ms": m, "positions": n_pos, "counts": counts}
+
+
+class _PlanLike:
+    """Minimal plan view for expected_positions from a materialised record."""
+
+    def __init__(self, rec):
+        self.R = rec["R"]
+        self._rates = rec["rates"]
+
+    def conditional_pass_rates(self):
+        return self._rates
+
+
+def collect(ks, procs: int | None = None, log=None, tune=None) -> list[dict]:
+    """Candidates for every k built in a process pool, probed one by one on the GPU."""
+    ctx = mp.get_context("spawn")
+    rows = []
+    with ctx.Pool(procs or os.cpu_count() or 4) as pool:
+        all_specs = [s for specs in pool.map(_specs_for, ks) for s in specs]
+        for rec in pool.imap(_materialise, all_specs, chunksize=4):
+            pr = probe(rec, tune)
+            epos = expected_positions(_PlanLike(rec), pr["counts"], pr["positions"])
+            row = {"k": rec["spec"]["k"], "wheel_name": rec["spec"]["wheel_name"],
+                   "order_name": rec["spec"]["order_name"], "ref_order": rec["ref_order"],
+                   "features": [float(x) for x in rec["features"]], "gcand": pr["gcand"],
+                   "log_tp": math.log(pr["gcand"]), "log_pos": math.log(epos),
+                   "true_cost": rec["true_cost"], "M_bits": rec["M_bits"], "R": rec["R"],
+                   "counts": pr["counts"][:8], "probe_positions": pr["positions"],
+                   "wheel": rec["spec"]["wheel"], "order": rec["spec"]["order"]}
+            rows.append(row)
+            if log and len(rows) % 200 == 0:
+                log(f"probed {len(rows)}/{len(all_specs)}")
+    return rows
+
+
+# ------------------------------------------------------------------ model fit and choice
+class CostModel:
+    """MLP on standardised features/targets; predicts (log throughput, log positions)."""
+
+    def __init__(self, seed: int = 0, hidden: int = 64):
+        self.seed, self.hidden = seed, hidden
+        self.mlp = None
+
+    def fit(self, rows, epochs: int = 600, batch: int = 256, lr: float = 2e-3) -> float:
+        X = np.array([r["features"] for r in rows], dtype=np.float64)
+        Y = np.array([[r["log_tp"], r["log_pos"]] for r in rows], dtype=np.float64)
+        self.xm, self.xs = X.mean(0), X.std(0) + 1e-6
+        self.ym, self.ys = Y.mean(0), Y.std(0) + 1e-6
+        self.mlp = MLP(X.shape[1], 2, self.hidden, self.seed)
+        return self.mlp.train((X - self.xm) / self.xs, (Y - self.ym) / self.ys, epochs, batch, lr, self.seed)
+
+    def predict(self, feats) -> np.ndarray:
+        X = (np.asarray(feats, dtype=np.float64) - self.xm) / self.xs
+        return self.mlp.forward(X).astype(np.float64) * self.ys + self.ym
+
+
+def split_ks(ks, held_out: int = 40, seed: int = 0):
+    rng = np.random.default_rng(seed)
+    ks = sorted(ks)
+    test = sorted(int(x) for x in rng.choice(ks, size=held_out, replace=False))
+    return [k for k in ks if k not in test], test
+
+
+def evaluate(rows, model: CostModel, test_ks) -> dict:
+    """Held-out comparison of the learned and the analytic planner."""
+    by_k = {}
+    for r in rows:
+        if r["k"] in test_ks:
+            by_k.setdefault(r["k"], []).append(r)
+    train_tp = [r["gcand"] for r in rows if r["k"] not in test_ks]
+    mean_tp = math.exp(statistics.fmean(math.log(x) for x in train_tp))
+    per_k, err_l, err_a, speed = {}, [], [], []
+    for k, cand in sorted(by_k.items()):
+        pred = model.predict([c["features"] for c in cand])
+        actual = [c["log_pos"] - c["log_tp"] for c in cand]            # ln(time) up to a constant
+        pred_l = [p[1] - p[0] for p in pred]
+        pred_a = [math.log(c["true_cost"]) - math.log(mean_tp) for c in cand]
+        for a, pl, pa in zip(actual, pred_l, pred_a):
+            err_l.append(abs(pl - a))
+            err_a.append(abs(pa - a))
+        ref = [i for i, c in enumerate(cand) if c["ref_order"]]
+        ia = min(ref, key=lambda i: cand[i]["true_cost"])             # analytic planner's choice
+        il = min(range(len(cand)), key=lambda i: pred_l[i])           # learned choice
+        ib = min(range(len(cand)), key=lambda i: actual[i])           # best measured
+        s = math.exp(actual[ia] - actual[il])
+        speed.append(s)
+        per_k[k] = {"analytic": f"{cand[ia]['wheel_name']}/{cand[ia]['order_name']}",
+                    "learned": f"{cand[il]['wheel_name']}/{cand[il]['order_name']}",
+                    "best": f"{cand[ib]['wheel_name']}/{cand[ib]['order_name']}",
+                    "time_ratio_analytic_over_learned": s,
+                    "time_ratio_analytic_over_best": math.exp(actual[ia] - actual[ib]),
+                    "analytic_gcand": cand[ia]["gcand"], "learned_gcand": cand[il]["gcand"]}
+    geo = math.exp(statistics.fmean(math.log(x) for x in speed)) if speed else None
+    return {"held_out_k": sorted(by_k), "n_candidates": sum(len(v) for v in by_k.values()),
+            "mae_log_time_learned": statistics.fmean(err_l) if err_l else None,
+            "mae_log_time_analytic": statistics.fmean(err_a) if err_a else None,
+            "geomean_time_ratio_analytic_over_learned": geo,
+            "min_time_ratio": min(speed) if speed else None, "per_k": per_k}
+
+
+def learned_order(model: CostModel, plan, seed: int = 0, tries: int = 48) -> list[int]:
+    """Cascade order with the least predicted time among candidate orders of one wheel."""
+    rng = np.random.default_rng(seed)
+    cands = [o for _, o in _orders(plan, rng)]
+    for _ in range(tries):
+        perm = list(plan.rest[:8])
+        rng.shuffle(perm)
+        cands.append(perm + list(plan.rest[8:]))
+    feats = [features(plan.with_order(o)) for o in cands]
+    pred = model.predict(feats)
+    best = min(range(len(cands)), key=lambda i: pred[i][1] - pred[i][0])
+    return cands[best]
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--n-k", type=int, default=200)
+    ap.add_argument("--held-out", type=int, default=40)
+    ap.add_argument("--dataset", default=None, help="probe rows (JSON); collected when missing")
+    ap.add_argument("--out", default=None)
+    ap.add_argument("--epochs", type=int, default=600)
+    a = ap.parse_args()
+    rng = np.random.default_rng(0)
+    ks = sorted(int(x) for x in rng.choice(np.arange(100, 401), size=a.n_k, replace=False))
+    t0 = time.time()
+    if a.dataset and os.path.exists(a.dataset):
+        rows = json.load(open(a.dataset))
+    else:
+        rows = collect(ks, log=lambda s: print(s, file=sys.stderr, flush=True))
+        if a.dataset:
+            json.dump(rows, open(a.dataset, "w"))
+    t_probe = time.time() - t0
+    train_ks, test_ks = split_ks(ks, a.held_out)
+    model = CostModel(0)
+    t1 = time.time()
+    loss = model.fit([r for r in rows if r["k"] in set(train_ks)], epochs=a.epochs)
+    t_train = time.time() - t1
+    rep = evaluate(rows, model, set(test_ks))
+    rep.update({"rows": len(rows), "probe_s": t_probe, "train_s": t_train, "train_loss": loss,
+                "epochs": a.epochs, "k_range": [min(ks), max(ks)]})
+    s = json.dumps(rep)
+    if a.out:
+        open(a.out, "w").write(s + "\n")
+    print(s)
+
+
+if __name__ == "__main__":
+    main()

@@ -139,6 +139,22 @@ def bit_table(q: int, residues) -> np.ndarray:
 class PlanArrays:
     """Flattened plan: ring terms (res * basis_j mod M), filter moduli and bit tables."""
 
+    @classmethod
+    def from_arrays(cls, k, radix, term_lo, term_hi, q, allowed, M) -> "PlanArrays":
+        """Rebuild from arrays produced elsewhere (e.g. a worker process)."""
+        self = object.__new__(cls)
+        mask64 = (1 << 64) - 1
+        self.radix, self.term_lo, self.term_hi = _u32(radix), _u64(term_lo), _u64(term_hi)
+        self.q, self.allowed = _u32(q), _u32(allowed)
+        n_rings = 0 if (self.radix.size == 1 and int(self.radix[0]) == 0) else self.radix.size
+        n_filters = 0 if (self.q.size == 1 and int(self.q[0]) == 0) else self.q.size
+        self.desc = PlanDesc(k=int(k), n_rings=n_rings, n_filters=n_filters, flags=0,
+                             M_lo=int(M) & mask64, M_hi=int(M) >> 64,
+                             radix=_ptr(self.radix, C.c_uint32), term_lo=_ptr(self.term_lo, C.c_uint64),
+                             term_hi=_ptr(self.term_hi, C.c_uint64), filter_q=_ptr(self.q, C.c_uint32),
+                             allowed=_ptr(self.allowed, C.c_uint32))
+        return self
+
     def __init__(self, plan):
         M = plan.M
         terms = []
@@ -182,10 +198,10 @@ def tconst_for(plan, t: int) -> np.ndarray:
 class Context:
     """One plan resident on the device (es_ctx)."""
 
-    def __init__(self, plan, tune: Tune | None = None, capacity: int | None = None):
+    def __init__(self, plan, tune: Tune | None = None, capacity: int | None = None, arrays=None):
         L = lib()
         self.plan = plan
-        self.arrays = PlanArrays(plan)
+        self.arrays = arrays if arrays is not None else PlanArrays(plan)
         self.tune = tune if tune is not None else make_tune()
         h = C.c_void_p()
         check(L.es_ctx_create(C.byref(self.arrays.desc), C.byref(self.tune), C.byref(h)))
@@ -197,6 +213,11 @@ class Context:
         if capacity is not None:
             self.set_capacity(capacity)
         self.t = 0
+
+    @classmethod
+    def from_arrays(cls, arrays: PlanArrays, tune: Tune | None = None, n_filters: int | None = None) -> "Context":
+        """A context built from flattened arrays only (no Plan object; set_block needs tconst)."""
+        return cls(None, tune, None, arrays)
 
     def close(self):
         if getattr(self, "h", None):

@@ -280,6 +280,14 @@ class Plan:
         self.density_wheel = self.R / self.M if self.M else 1.0
         self.density_rest = self.density_all / self.density_wheel
 
+    def with_order(self, order) -> "Plan":
+        """A copy of this plan with another cascade order (same wheel, rings and basis)."""
+        assert sorted(order) == sorted(self.rest), "filter order is not a permutation"
+        q = object.__new__(type(self))
+        q.__dict__.update(self.__dict__)
+        q.rest = [int(p) for p in order]
+        return q
+
     # -------------------------------------------------------------- index <-> n
     def terms(self) -> list[list[int]]:
         """Per ring j: (residue * basis_j) mod M for each residue, in ring order."""

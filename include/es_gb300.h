@@ -183,6 +183,22 @@ int es_search_blocks_static(const es_ctx* ctx, uint64_t t0, uint32_t n_blocks, e
                             uint64_t out_cap, unsigned long long* d_count, unsigned long long* d_min,
                             void* stream);
 
+/* ---- learned planner: 3-layer FP32 MLP trained and evaluated by this library's kernels -------
+ * No counterpart in the reference: it stands in for the knapsack planner's analytic cost
+ * estimate (sieve/gpu_sieve_v9.py:187-227 ranks wheels by expected checks only).  Parameters are
+ * flat FP32: W1[H][D], b1[H], W2[H][H], b2[H], W3[O][H], b3[O]; loss = mean squared error. */
+typedef struct es_mlp es_mlp;
+const char* es_mlp_last_error(void);
+int es_mlp_create(uint32_t in_dim, uint32_t hidden, uint32_t out_dim, uint64_t seed, es_mlp** out);
+int es_mlp_destroy(es_mlp* m);
+int es_mlp_num_params(const es_mlp* m, uint64_t* n);
+int es_mlp_get_params(es_mlp* m, float* out, uint64_t n);
+int es_mlp_set_params(es_mlp* m, const float* in, uint64_t n);   /* also resets the optimiser */
+int es_mlp_forward(es_mlp* m, const float* X, uint64_t n, float* Y);
+int es_mlp_loss_grad(es_mlp* m, const float* X, const float* T, uint64_t n, float* loss, float* grad);
+int es_mlp_train(es_mlp* m, const float* X, const float* T, uint64_t n, uint32_t epochs,
+                 uint32_t batch, float lr, uint64_t seed, float* final_loss);
+
 /* ---- measurement -------------------------------------------------------------------------- */
 /* Integer-pipe peak microbenchmark: int32 operations per second of a dependent-free mix of
  * IADD3 / LOP3 / IMAD-class instructions across the whole GPU (ops = lanes x instructions). */
