@@ -177,9 +177,30 @@ def k390(log2_positions: int = 40, filter_orders: dict | None = None, tune: dict
             "cross_checked": True, "disagreements": disagree}
 
 
+def k390_learned(model_path: str, log2_positions: int = 40, reps: int = 2) -> dict:
+    """The k = 390 fixed-scope confirmation scan with the learned cascade order of each wheel
+    against the same scan in the analytic (reference) order."""
+    import es_learned
+    model = es_learned.CostModel.load(model_path)
+    orders, names = {}, {}
+    for role, wheel in K390_WHEELS.items():
+        P = es_gb300.Plan(390, None, wheel)
+        names[role], orders[role] = es_learned.learned_order(model, P)
+    learned = k390(log2_positions, filter_orders=orders, reps=reps)
+    analytic = k390(log2_positions, reps=reps)
+    same = all(learned["wheels"][r]["survivors_n"] == analytic["wheels"][r]["survivors_n"]
+               for r in K390_WHEELS)
+    return {"learned_orders": names, "learned_ms": learned["ms"], "analytic_ms": analytic["ms"],
+            "learned_Gcand_s": learned["Gcand_s"], "analytic_Gcand_s": analytic["Gcand_s"],
+            "wall_ratio_analytic_over_learned": analytic["ms"] / learned["ms"],
+            "survivors_identical": same, "disagreements": learned["disagreements"] + analytic["disagreements"],
+            "learned": learned, "analytic": analytic}
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("which", choices=["small-k", "batch64", "k390"])
+    ap.add_argument("which", choices=["small-k", "batch64", "k390", "k390-learned"])
+    ap.add_argument("--model", default=None, help="learned cost model (es_learned.py --save-model)")
     ap.add_argument("--json", default=None)
     ap.add_argument("--bfile", default=None)
     ap.add_argument("--log2-positions", type=int, default=40)
@@ -190,8 +211,10 @@ def main():
         out = small_k(known=known)
     elif a.which == "batch64":
         out = batch64(autotune=not a.no_autotune)
-    else:
+    elif a.which == "k390":
         out = k390(a.log2_positions)
+    else:
+        out = k390_learned(a.model, a.log2_positions)
     s = json.dumps(out, default=str)
     if a.json:
         with open(a.json, "w") as f:

@@ -40,6 +40,7 @@ if HERE not in sys.path:
 import es_plan  # noqa: E402
 
 N_FIRST = 6          # filters described individually in the features
+MODEL_PATH = os.path.join(HERE, "data", "cost_model.json")   # trained on 160 k of 100..400
 FEATURE_DIM = 14 + 3 * N_FIRST
 PROBE_LOG2 = 28
 
@@ -188,20 +189,33 @@ WHEEL_TUNES = [
 ]
 
 
-def _orders(plan, rng) -> list[tuple[str, list[int]]]:
+def _orders(plan, rng, shuffles: int = 2) -> list[tuple[str, list[int]]]:
+    """Cascade-order families: the reference order, orders that trade rejection against the
+    word-mask table footprint (several L1 budgets), small-q-first heads, and random heads."""
     ref = list(plan.rest)
     out = [("reference", ref)]
     W = ((plan.radix[0] if plan.radix else 1) + 31) // 32
     rates = dict(zip(ref, plan.conditional_pass_rates()))
-    # table-aware: rejection per unit of word-mask table footprint for the first slots
-    def score(p):
-        q = plan.info[p][0]
-        return (1.0 - rates[p]) / (1.0 + q * W * 4 / 65536.0)
-    head = sorted(ref, key=score, reverse=True)[:N_FIRST]
-    out.append(("table-aware", head + [p for p in ref if p not in head]))
-    small = sorted(ref[:8], key=lambda p: plan.info[p][0])
-    out.append(("small-q-first", small + ref[8:]))
-    for i in range(3):
+    size = {p: plan.info[p][0] * W * 4 for p in ref}
+
+    def rest_after(head):
+        hs = set(head)
+        return head + [p for p in ref if p not in hs]
+    # rejection per unit of table footprint, at three penalty scales
+    for name, scale in (("table-aware-16k", 16384.0), ("table-aware", 65536.0), ("table-aware-256k", 262144.0)):
+        head = sorted(ref, key=lambda p: (1.0 - rates[p]) / (1.0 + size[p] / scale), reverse=True)[:N_FIRST]
+        out.append((name, rest_after(head)))
+    # greedy: most rejection among the first four within an L1 budget, the rest by pass rate
+    for name, budget in (("l1-96k", 96 * 1024), ("l1-160k", 160 * 1024)):
+        head, used = [], 0
+        for p in sorted(ref, key=lambda p: rates[p]):
+            if len(head) < 4 and used + size[p] <= budget:
+                head.append(p)
+                used += size[p]
+        out.append((name, rest_after(head)))
+    out.append(("small-q-first", sorted(ref[:8], key=lambda p: plan.info[p][0]) + ref[8:]))
+    out.append(("small-q-first-4", sorted(ref[:4], key=lambda p: plan.info[p][0]) + ref[4:]))
+    for i in range(shuffles):
         perm = ref[:8]
         rng.shuffle(perm)
         out.append((f"shuffle{i}", perm + ref[8:]))
@@ -255,9 +269,10 @@ def _specs_for(k):
 
 
 # ------------------------------------------------------------------ GPU probes
-def probe(item: dict, tune=None, log2_pos: int = PROBE_LOG2, reps: int = 3) -> dict:
+def probe(item: dict, tune=None, log2_pos: int | None = None, reps: int = 3) -> dict:
     """Time 2^log2_pos positions of block 0 (median of reps) and take stage counts once."""
     import es_native as N
+    log2_pos = PROBE_LOG2 if log2_pos is None else log2_pos
     k, radix, lo, hi, q, allowed, M = item["arrays"]
     A = N.PlanArrays.from_arrays(k, radix, lo, hi, q, allowed, M)
     t = N.make_tune(**dict(tune or {}, count_stages=1))
@@ -337,6 +352,22 @@ class CostModel:
         X = (np.asarray(feats, dtype=np.float64) - self.xm) / self.xs
         return self.mlp.forward(X).astype(np.float64) * self.ys + self.ym
 
+    def save(self, path: str) -> None:
+        json.dump({"feature_dim": FEATURE_DIM, "hidden": self.hidden, "seed": self.seed,
+                   "xm": self.xm.tolist(), "xs": self.xs.tolist(), "ym": self.ym.tolist(),
+                   "ys": self.ys.tolist(), "params": self.mlp.params().tolist()}, open(path, "w"))
+
+    @classmethod
+    def load(cls, path: str) -> "CostModel":
+        d = json.load(open(path))
+        assert d["feature_dim"] == FEATURE_DIM, "model was trained on another feature set"
+        m = cls(d["seed"], d["hidden"])
+        m.xm, m.xs = np.array(d["xm"]), np.array(d["xs"])
+        m.ym, m.ys = np.array(d["ym"]), np.array(d["ys"])
+        m.mlp = MLP(FEATURE_DIM, 2, d["hidden"], d["seed"])
+        m.mlp.set_params(np.array(d["params"], dtype=np.float32))
+        return m
+
 
 def split_ks(ks, held_out: int = 40, seed: int = 0):
     rng = np.random.default_rng(seed)
@@ -375,23 +406,34 @@ def evaluate(rows, model: CostModel, test_ks) -> dict:
                     "time_ratio_analytic_over_best": math.exp(actual[ia] - actual[ib]),
                     "analytic_gcand": cand[ia]["gcand"], "learned_gcand": cand[il]["gcand"]}
     geo = math.exp(statistics.fmean(math.log(x) for x in speed)) if speed else None
+    # fixed-scope scans (fixed positions, the default wheel): the learned order's measured
+    # throughput against the reference order's; positions are equal, so time ratio = rate ratio
+    fixed = []
+    for k, cand in sorted(by_k.items()):
+        dw = [c for c in cand if c["wheel_name"] == "default"]
+        ref = [c for c in dw if c["ref_order"]]
+        if not dw or not ref:
+            continue
+        pred = model.predict([c["features"] for c in dw])
+        il = max(range(len(dw)), key=lambda i: pred[i][0])
+        fixed.append(dw[il]["gcand"] / ref[0]["gcand"])
+        per_k[k]["fixed_scope_learned_order"] = dw[il]["order_name"]
+        per_k[k]["fixed_scope_time_ratio"] = fixed[-1]
+    geo_fixed = math.exp(statistics.fmean(math.log(x) for x in fixed)) if fixed else None
     return {"held_out_k": sorted(by_k), "n_candidates": sum(len(v) for v in by_k.values()),
+            "fixed_scope_geomean_time_ratio_reference_over_learned_order": geo_fixed,
             "mae_log_time_learned": statistics.fmean(err_l) if err_l else None,
             "mae_log_time_analytic": statistics.fmean(err_a) if err_a else None,
             "geomean_time_ratio_analytic_over_learned": geo,
             "min_time_ratio": min(speed) if speed else None, "per_k": per_k}
 
 
-def learned_order(model: CostModel, plan, seed: int = 0, tries: int = 48) -> list[int]:
-    """Cascade order with the least predicted time among candidate orders of one wheel."""
+def learned_order(model: CostModel, plan, seed: int = 0) -> tuple[str, list[int]]:
+    """Cascade order of one wheel with the least predicted time among the order families the
+    model was trained on (a fixed-scope scan has fixed positions, so this is the fastest order)."""
     rng = np.random.default_rng(seed)
-    cands = [o for _, o in _orders(plan, rng)]
-    for _ in range(tries):
-        perm = list(plan.rest[:8])
-        rng.shuffle(perm)
-        cands.append(perm + list(plan.rest[8:]))
-    feats = [features(plan.with_order(o)) for o in cands]
-    pred = model.predict(feats)
+    cands = [(n, o) for n, o in _orders(plan, rng, shuffles=0)]
+    pred = model.predict([features(plan.with_order(o)) for _, o in cands])
     best = min(range(len(cands)), key=lambda i: pred[i][1] - pred[i][0])
     return cands[best]
 
@@ -403,6 +445,7 @@ def main():
     ap.add_argument("--dataset", default=None, help="probe rows (JSON); collected when missing")
     ap.add_argument("--out", default=None)
     ap.add_argument("--epochs", type=int, default=600)
+    ap.add_argument("--save-model", default=None, help="write the trained model (JSON) here")
     a = ap.parse_args()
     rng = np.random.default_rng(0)
     ks = sorted(int(x) for x in rng.choice(np.arange(100, 401), size=a.n_k, replace=False))
@@ -420,6 +463,8 @@ def main():
     loss = model.fit([r for r in rows if r["k"] in set(train_ks)], epochs=a.epochs)
     t_train = time.time() - t1
     rep = evaluate(rows, model, set(test_ks))
+    if a.save_model:
+        model.save(a.save_model)
     rep.update({"rows": len(rows), "probe_s": t_probe, "train_s": t_train, "train_loss": loss,
                 "epochs": a.epochs, "k_range": [min(ks), max(ks)]})
     s = json.dumps(rep)

@@ -1,0 +1,41 @@
+"""GPU: what the trained cost model gains over the analytic planner.
+
+A small seeded campaign (24 k in 100..400, every candidate plan probed on 2^26 positions of
+block 0) is collected on the GPU, the MLP is trained by the library's CUDA kernels on 18 k,
+and on the 6 held-out k (a) its time prediction error is compared with the analytic model's
+(expected checks at the mean training rate) and (b) its plan choices are compared with the
+analytic planner's choices by measured time to completion."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def test_learned_model_beats_analytic_on_held_out_k(native):
+    import es_learned
+    es_learned.PROBE_LOG2 = 26
+    rng = np.random.default_rng(7)
+    ks = sorted(int(x) for x in rng.choice(np.arange(100, 401), size=24, replace=False))
+    rows = es_learned.collect(ks, procs=8)
+    assert len(rows) > 24 * 20
+    train, test = es_learned.split_ks(ks, held_out=6, seed=1)
+    model = es_learned.CostModel(0)
+    model.fit([r for r in rows if r["k"] in set(train)], epochs=400)
+    rep = es_learned.evaluate(rows, model, set(test))
+    assert rep["mae_log_time_learned"] < 0.6 * rep["mae_log_time_analytic"], rep
+    assert rep["geomean_time_ratio_analytic_over_learned"] >= 1.0, rep
+
+
+def test_packaged_model_orders_are_permutations(native):
+    """The committed model loads, runs on the GPU and proposes valid cascade orders."""
+    import os
+    import es_gb300
+    import es_learned
+    path = os.path.join(os.path.dirname(es_learned.__file__), "data", "cost_model.json")
+    model = es_learned.CostModel.load(path)
+    for k in (150, 300, 390):
+        P = es_gb300.Plan(k)
+        name, order = es_learned.learned_order(model, P)
+        assert sorted(order) == sorted(P.rest)
+        pred = model.predict([es_learned.features(P)])
+        assert np.all(np.isfinite(pred))
