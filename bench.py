@@ -37,6 +37,10 @@ for _p in (PKG, ORACLE):
 
 K_BENCH = 300
 LOG2_POS = 34
+# DRAM bytes per scan launch of this workload (dram__bytes_read.sum + dram__bytes_write.sum, one
+# ncu capture on GB300 of the 2^30-position case): the scan reads only its plan tables, once, so
+# the figure does not grow with the range (algorithmic HBM bytes per candidate: zero).
+TABLE_TRAFFIC_BYTES = 265216 + 768
 METRIC = "Gcand/s on 1 GB300 (% int peak)"
 
 
@@ -297,7 +301,7 @@ def main():
                 "d2h_bytes_per_step": 8 + 40 * n_e, "ms_per_step": e2e_step_ms},
         "gpu_launches": args.steps,
         "roofline": {"bound": "int32", "achieved": achieved, "peak": peak, "unit": "Tops/s",
-                     "frac": achieved / peak, "traffic": None,
+                     "frac": achieved / peak, "traffic": TABLE_TRAFFIC_BYTES,
                      "model": f"W=10+8*fbar int32 ops/candidate, fbar={fbar:.4f} (this run's stage counts)",
                      "peak_source": "measured: es_int_peak IADD3/LOP3 microbenchmark, this run"},
         "clocks": clocks,
@@ -307,6 +311,29 @@ def main():
         "wall_s_timed_region": wall,
         "device": dev,
     }
+    # the same fixed-scope scan in the learned cascade order (packaged cost model); the headline
+    # stays in the reference order, whose per-stage counts the parity tests pin
+    try:
+        import es_learned
+        model = es_learned.CostModel.load(es_learned.MODEL_PATH)
+        oname, order = es_learned.learned_order(model, plan)
+        lctx = N.Context(plan.with_order(order), sieve.tune)
+        lctx.set_block(0)
+        for _ in range(3):
+            lctx.reset()
+            lctx.launch_timed(o_begin, n_outer)
+        lms = []
+        for _ in range(max(3, min(args.steps, 10))):
+            flush.zero_()
+            torch.cuda.synchronize()
+            lctx.reset()
+            lms.append(lctx.launch_timed(o_begin, n_outer))
+        lctx.close()
+        l_ms = max_over_ranks(pg, statistics.mean(lms))
+        line["learned_order"] = {"order": oname, "value": world * n_pos / (l_ms * 1e-3) / 1e9, "unit": "Gcand/s",
+                                 "ms_per_step": l_ms, "time_ratio_reference_over_learned": ms_step / l_ms}
+    except Exception as e:  # the learned model is optional for the headline
+        line["learned_order"] = {"error": str(e)[:200]}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         outer = cpu_sample(plan)
         v_py, cores, dt_py = cpu_baseline_py(plan, outer)
