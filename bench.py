@@ -174,6 +174,8 @@ def run_reference(args, rank, world, pg):
     import es_gb300
     plan = es_gb300.Plan(K_BENCH)
     outer = cpu_sample(plan)
+    if args.steps > 30:   # keep the whole run within a few minutes: a smaller sample per step
+        outer = outer[: max(4096, outer.size * 30 // args.steps)]
     for _ in range(max(0, min(args.warmup, 1))):
         cpu_baseline_py(plan, outer[:20000])
     vals = []
@@ -187,8 +189,10 @@ def run_reference(args, rank, world, pg):
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "Gcand/s", "n_gpus": 0,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "int (exact)", "data": "synthetic",
-            "config": {"workload": "k=300 Plan(300) default wheel, block 0, seeded 2^24-position sample "
-                                   "(2^19 outer indices of [0,2^34)/32 x inner ring)", "k": K_BENCH},
+            "config": {"workload": f"k=300 fixed-scope scan: Plan(300) default wheel (M=2^95, r0=32, "
+                                   f"{len(plan.rest)} filters), block 0, positions [0, 2^{LOG2_POS}); timed on "
+                                   f"a seeded sample of {outer.size * 32} positions (2^19 outer indices of "
+                                   f"[0,2^34)/32 x the inner ring)", "k": K_BENCH},
             "cpu_baseline": {"value": v, "unit": "Gcand/s", "cores": os.cpu_count(), "kind": "port",
                              "sample": f"{outer.size * 32} positions per step (seeded sample of the "
                                        "k=300 workload), Python restatement of the reference CPU path, "

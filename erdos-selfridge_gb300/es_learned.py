@@ -382,8 +382,8 @@ def evaluate(rows, model: CostModel, test_ks) -> dict:
     for r in rows:
         if r["k"] in test_ks:
             by_k.setdefault(r["k"], []).append(r)
-    train_tp = [r["gcand"] for r in rows if r["k"] not in test_ks]
-    mean_tp = math.exp(statistics.fmean(math.log(x) for x in train_tp))
+    # the analytic model's rate: the geometric-mean throughput of the model's training set
+    mean_tp = math.exp(float(model.ym[0]))
     per_k, err_l, err_a, speed = {}, [], [], []
     for k, cand in sorted(by_k.items()):
         pred = model.predict([c["features"] for c in cand])
