@@ -170,8 +170,8 @@ struct SmemPlan {
     uint32_t fast_words_cap;
 };
 
-// per-warp survivor queue (64 entries x 24 bytes), must match the kernel's EsQueue
-constexpr uint32_t kQueueBytes = 64u * 24u;
+// per-warp survivor queue (64 entries x 28 bytes), must match the kernel's EsQueue
+constexpr uint32_t kQueueBytes = 64u * 28u;
 
 SmemPlan plan_smem(uint32_t small_max, uint32_t nf_max, const es_tune& tune, uint32_t fast_need) {
     SmemPlan p;
@@ -373,6 +373,7 @@ int es_ctx_create(const es_plan_desc* d, const es_tune* tune_in, es_ctx** out) {
     I.o_Q0 = take(4ull * ES_FMAX * r0);
     I.o_BK = take(2ull * (ES_NBUCKET + 1));
     I.o_FC = take(sizeof(EsFilterC) * std::max<uint32_t>(nf, 1));
+    I.o_K1 = take(4ull * r1);
     const size_t small_bytes = off;
     std::vector<unsigned char> small(small_bytes, 0);
     auto put128 = [&](uint32_t o, uint32_t i, u128 v) {
@@ -384,6 +385,7 @@ int es_ctx_create(const es_plan_desc* d, const es_tune* tune_in, es_ctx** out) {
     for (uint32_t i = 0; i < r1; ++i) {
         const u128 v = terms[roff[1] + i];
         put128(I.o_T1, i, v);
+        put32(I.o_K1, i, (uint32_t)(v >> sh));
         for (uint32_t f = 0; f < FB; ++f) put32(I.o_TQ1, i * ES_FMAX + f, mod_q(v, c->q[f]));
     }
     for (uint32_t i = 0; i < r2; ++i) {
@@ -460,6 +462,7 @@ int es_ctx_create(const es_plan_desc* d, const es_tune* tune_in, es_ctx** out) {
     I.sh = sh;
     I.bsh = bsh;
     I.tail_mask = (r0 % 32) ? ((1u << (r0 % 32)) - 1u) : 0xffffffffu;
+    I.km = (uint32_t)(M >> sh);
     I.small_bytes = (uint32_t)small_bytes;
     for (uint32_t f = 0; f <= ES_FMAX; ++f) I.mask_off[f] = mask_off[f];
     I.small = c->d_arena + a_small;

@@ -3,6 +3,7 @@
 // Data layout in HBM (one arena per plan context, uploaded once):
 //   small block   contiguous tables staged verbatim into shared memory by every CTA:
 //                   T1[r1]      ring-1 terms (128-bit)                      16 B each
+//                   K1[r1]      32-bit keys of T1 (ring-1 wrap and split keys) 4 B each
 //                   TQ1[r1][8]  ring-1 terms mod q_f, f < 8                  32 B each
 //                   D2[r2]      ring-2 step deltas term2[d+1]-term2[d] mod M 16 B each
 //                   DQ2[r2][8]  those deltas mod q_f                        32 B each
@@ -47,8 +48,9 @@ struct EsInst {
     uint32_t bsh;         // bucket shift: bucket = key >> bsh
     uint32_t tail_mask;   // valid bits of the last inner word
     uint32_t small_bytes; // size of the small block (multiple of 16)
+    uint32_t km;          // M >> sh (32-bit key of M)
     // byte offsets inside the small block
-    uint32_t o_T1, o_TQ1, o_D2, o_DQ2, o_S0, o_K0, o_I0, o_Q0, o_BK, o_FC;
+    uint32_t o_T1, o_TQ1, o_D2, o_DQ2, o_S0, o_K0, o_I0, o_Q0, o_BK, o_FC, o_K1;
     // word offsets of the fast (word-mask) tables, F_built + 1 entries (prefix sums)
     uint32_t mask_off[ES_FMAX + 1];
     uint32_t pad0;

@@ -143,8 +143,9 @@ __device__ __forceinline__ void copy_words(uint32_t* dst, const uint32_t* __rest
 // on 32 queued candidates at a time so that whole warps, not single lanes, do the 128-bit work.
 #define ES_QCAP 64
 struct EsQueue {
-    uint4 s[ES_QCAP];                  // n mod M, 32-bit limbs
-    unsigned long long idx[ES_QCAP];   // block-relative position index
+    uint4 b2[ES_QCAP];                 // sum of the ring >= 2 terms mod M (32-bit limbs)
+    unsigned long long oidx[ES_QCAP];  // outer index
+    uint32_t info[ES_QCAP];            // sorted inner slot | ring-1 digit << 16
 };
 
 __device__ __forceinline__ void red_add_shared(uint32_t saddr, uint32_t v) {
@@ -178,6 +179,9 @@ struct TailCtx {
     U4 M;
     uint64_t M_lo;
     uint64_t t_blk;
+    const uint4* sT1;          // ring-1 terms (shared)
+    const uint4* sS0;          // sorted inner-ring terms (shared)
+    const uint32_t* sI0;       // original inner digit of each sorted slot (shared)
     const EsFilterC* sFC;
     const uint32_t* tc;
     const uint32_t* allowed_g;
@@ -185,9 +189,19 @@ struct TailCtx {
     unsigned long long* surv_n;
     unsigned long long* group_found;
     uint64_t surv_cap;
-    uint32_t kp1, Feff, nf, wcnt_saddr, item_id, group;
+    uint32_t kp1, Feff, nf, wcnt_saddr, item_id, group, r0;
     bool M_big;
 };
+
+// n mod M and the position index of queued candidate (b2, oidx, slot, d1)
+__device__ __forceinline__ void rebuild(const TailCtx& C, const U4 b2, uint64_t oidx, uint32_t info,
+                                        U4& s, uint64_t& idx) {
+    const uint32_t slot = info & 0xffffu, d1 = info >> 16;
+    uint32_t wm;
+    const U4 b = addmod(b2, u4(C.sT1[d1]), C.M, wm);
+    s = addmod(b, u4(C.sS0[slot]), C.M, wm);
+    idx = oidx * (uint64_t)C.r0 + C.sI0[slot];
+}
 
 // exact tail of the cascade for one candidate (filters Feff..nf-1), then the emit
 template <bool COUNT>
@@ -228,26 +242,39 @@ __device__ __forceinline__ void flush(const TailCtx& C, EsQueue* Q, uint32_t lan
     const uint32_t n = qsize < 32u ? qsize : 32u;
     if (lane < n) {
         const uint32_t e = (qhead + lane) & (ES_QCAP - 1);
-        tail_one<COUNT>(C, u4(Q->s[e]), Q->idx[e]);
+        U4 s;
+        uint64_t idx;
+        rebuild(C, u4(Q->b2[e]), Q->oidx[e], Q->info[e], s, idx);
+        tail_one<COUNT>(C, s, idx);
     }
     qhead = (qhead + n) & (ES_QCAP - 1);
     qsize -= n;
     __syncwarp();
 }
 
-// warp-uniform: queue the set bits of one inner word (sorted slots base + i)
+// warp-uniform: queue the set bits of one inner word (sorted slots base + i) of outer index
+// oidx = c * r1 + d1; only (b2, oidx, slot, d1) are stored, n mod M is rebuilt at the flush
 template <bool COUNT>
 __device__ __forceinline__ void push(const TailCtx& C, EsQueue* Q, uint32_t lane, uint32_t& qhead,
-                                     uint32_t& qsize, uint32_t bits, uint32_t base, const U4 b,
-                                     uint64_t obase, const uint4* sS0, const uint32_t* sI0) {
+                                     uint32_t& qsize, uint32_t bits, uint32_t base, const U4 b2,
+                                     uint64_t oidx, uint32_t d1) {
     const uint32_t n = __popc(bits);
-    uint32_t incl = n;
+    uint32_t excl, tot;
+    if (__ballot_sync(0xffffffffu, n > 1u) == 0u) {
+        // common case: at most one candidate per lane
+        const uint32_t has = __ballot_sync(0xffffffffu, n != 0u);
+        excl = __popc(has & ((1u << lane) - 1u));
+        tot = __popc(has);
+    } else {
+        uint32_t incl = n;
 #pragma unroll
-    for (uint32_t o = 1; o < 32; o <<= 1) {
-        const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += v;
+        for (uint32_t o = 1; o < 32; o <<= 1) {
+            const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        excl = incl - n;
+        tot = __shfl_sync(0xffffffffu, incl, 31);
     }
-    const uint32_t tot = __shfl_sync(0xffffffffu, incl, 31);
     if (qsize + tot > ES_QCAP)
         while (qsize) flush<COUNT>(C, Q, lane, qhead, qsize);
     if (tot > ES_QCAP) {
@@ -255,23 +282,21 @@ __device__ __forceinline__ void push(const TailCtx& C, EsQueue* Q, uint32_t lane
         while (bits) {
             const uint32_t i = __ffs(bits) - 1u;
             bits &= bits - 1u;
-            const uint32_t slot = base + i;
-            uint32_t wm;
-            const U4 s = addmod(b, u4(sS0[slot]), C.M, wm);
-            tail_one<COUNT>(C, s, obase + sI0[slot]);
+            U4 s;
+            uint64_t idx;
+            rebuild(C, b2, oidx, (base + i) | (d1 << 16), s, idx);
+            tail_one<COUNT>(C, s, idx);
         }
         return;
     }
-    uint32_t pos = qhead + qsize + incl - n;
+    uint32_t pos = qhead + qsize + excl;
     while (bits) {
         const uint32_t i = __ffs(bits) - 1u;
         bits &= bits - 1u;
-        const uint32_t slot = base + i;
-        uint32_t wm;
-        const U4 s = addmod(b, u4(sS0[slot]), C.M, wm);
         const uint32_t qe = pos & (ES_QCAP - 1);
-        Q->s[qe] = make_uint4(s.x, s.y, s.z, s.w);
-        Q->idx[qe] = obase + sI0[slot];
+        Q->b2[qe] = make_uint4(b2.x, b2.y, b2.z, b2.w);
+        Q->oidx[qe] = oidx;
+        Q->info[qe] = (base + i) | (d1 << 16);
         ++pos;
     }
     qsize += tot;
@@ -290,6 +315,10 @@ __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, u
     C.kp1 = si.k + 1u;
     C.M_big = (si.M_hi != 0) || (si.M_lo > C.kp1);
     C.nf = si.n_filters;
+    C.r0 = si.r0;
+    C.sT1 = reinterpret_cast<const uint4*>(smem + si.o_T1);
+    C.sS0 = reinterpret_cast<const uint4*>(smem + si.o_S0);
+    C.sI0 = reinterpret_cast<const uint32_t*>(smem + si.o_I0);
     C.sFC = reinterpret_cast<const EsFilterC*>(smem + si.o_FC);
     C.tc = L.items ? item.tconst : L.tconst0;
     C.allowed_g = si.allowed;
@@ -316,6 +345,8 @@ __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, u
     const uint32_t* sI0 = reinterpret_cast<const uint32_t*>(smem + si.o_I0);
     const uint32_t* sQ0 = reinterpret_cast<const uint32_t*>(smem + si.o_Q0);
     const uint16_t* sBK = reinterpret_cast<const uint16_t*>(smem + si.o_BK);
+    const uint32_t* sK1 = reinterpret_cast<const uint32_t*>(smem + si.o_K1);
+    const uint32_t KM = si.km;
     const uint64_t ob = item.o_begin, oe = item.o_end;
     const uint64_t* list = item.list;
     // word-mask: exactly F filters in the inner-ring stage (the host guarantees F <= filters and
@@ -398,34 +429,51 @@ __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, u
             }
             prev_c = c;
         }
+        // A = M - b2 and its 32-bit key, once per ring-1 cycle
+        uint32_t brA;
+        const U4 A = sub128(M, b2, brA);
+        const uint32_t KA = __funnelshift_r(kl == 0 ? A.x : (kl == 1 ? A.y : A.z),
+                                            kl == 0 ? A.y : (kl == 1 ? A.z : A.w), ko);
 
         // ---- ring 1: warp-uniform sweep (broadcast loads) --------------------------------
         for (uint32_t d1 = 0; d1 < r1; ++d1) {
-            const bool act = (d1 >= lo1) && (d1 < hi1);
-            uint32_t wm1;
-            const U4 b = addmod(b2, u4(sT1[d1]), M, wm1);
+            const bool act = (d1 - lo1) < (hi1 - lo1);          // lo1 <= d1 < hi1
+            // ring-1 wrap (b2 + T1 >= M, i.e. T1 >= A) from the 32-bit keys
+            const uint32_t k1 = sK1[d1];
+            uint32_t wm1 = k1 > KA ? 0xffffffffu : 0u;
             uint32_t tq[8];
             row8<F>(sTQ1 + d1 * (ES_FMAX / 4), tq);
-            // carry split: sorted slots [split, r0) wrap past M (sentinels at r0)
-            uint32_t brw;
-            const U4 thr = sub128(M, b, brw);
-            const uint32_t klo = kl == 0 ? thr.x : (kl == 1 ? thr.y : thr.z);
-            const uint32_t khi = kl == 0 ? thr.y : (kl == 1 ? thr.z : thr.w);
-            const uint32_t t32 = __funnelshift_r(klo, khi, ko);
-            uint32_t split = sBK[t32 >> bsh];
-            split += (sK0[split] < t32) ? 1u : 0u;
-            split += (sK0[split] < t32) ? 1u : 0u;
-            if (sK0[split] <= t32) {
-                while (sK0[split] < t32) ++split;
-                while (sK0[split] == t32 && lt128(u4(sS0[split]), thr)) ++split;
+            // carry split of the inner ring: slots [split, r0) wrap past M.  Away from a key tie,
+            // t is the key of thr = M - b to within +-1 and fits 32 bits (0 <= t <= KM); keys
+            // below t-1 are certainly below thr, keys above t+1 certainly not.
+            const uint32_t t = wm1 ? KM - (k1 - KA) : KA - k1;
+            const uint32_t tl = max(t, 1u) - 1u;
+            const uint32_t th = min(t, 0xfffffffeu) + 1u;
+            uint32_t split = sBK[tl >> bsh];
+            split += (sK0[split] < tl) ? 1u : 0u;
+            split += (sK0[split] < tl) ? 1u : 0u;
+            // rare: a key tie with A, a key inside the +-1 band, or a crowded bucket -> exact
+            const bool rare = (k1 == KA) || (sK0[split] <= th);
+            if (__any_sync(0xffffffffu, rare)) {
+                if (rare) {
+                    uint32_t wx, brw;
+                    const U4 b = addmod(b2, u4(sT1[d1]), M, wx);
+                    wm1 = wx;
+                    const U4 thr = sub128(M, b, brw);
+                    const uint32_t te = __funnelshift_r(kl == 0 ? thr.x : (kl == 1 ? thr.y : thr.z),
+                                                        kl == 0 ? thr.y : (kl == 1 ? thr.z : thr.w), ko);
+                    split = sBK[te >> bsh];
+                    while (sK0[split] < te) ++split;
+                    while (sK0[split] == te && lt128(u4(sS0[split]), thr)) ++split;   // S0[r0] = M stops it
+                }
             }
 
             for (uint32_t wd = 0; wd < Wn; ++wd) {
                 const uint32_t valid = (wd + 1u == Wn) ? tail : 0xffffffffu;
                 uint32_t bits = act ? valid : 0u;
                 const uint32_t base = wd << 5;
-                const uint32_t cm = split <= base ? valid
-                                  : (split >= base + 32u ? 0u : ((0xffffffffu << (split - base)) & valid));
+                // slots >= split of this word wrap: all-ones shifted left by (split - base) in [0, 32]
+                const uint32_t cm = __funnelshift_lc(0u, 0xffffffffu, max(split, base) - base) & valid;
                 if (LAYOUT == ES_LAYOUT_WORDMASK) {
                     // straight-line cascade: two table loads per filter per 32 candidates
 #pragma unroll
@@ -460,7 +508,7 @@ __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, u
                 }
                 // ---- queue the survivors of the inner-ring stage -----------------------------
                 if (__ballot_sync(0xffffffffu, bits != 0u))
-                    push<COUNT>(C, Q, lane, qhead, qsize, bits, base, b, (c * r1 + d1) * (uint64_t)r0, sS0, sI0);
+                    push<COUNT>(C, Q, lane, qhead, qsize, bits, base, b2, c * r1 + d1, d1);
             }
         }
     }

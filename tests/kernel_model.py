@@ -29,22 +29,46 @@ class KernelModel:
         kb = (M >> self.sh).bit_length()
         self.bsh = kb - 10 if kb > 10 else 0
         self.BK = [sum(1 for x in self.K0[:-1] if x < (b << self.bsh)) for b in range(1025)]
+        self.K1 = [v >> self.sh for v in terms[1]]       # 32-bit keys of the ring-1 terms
+        self.KM = M >> self.sh
+        self.exact_fallbacks = 0
         self.q = [plan.info[p][0] for p in plan.rest]
         self.ok = [set(plan.info[p][1]) for p in plan.rest]
         self.corr = [(q - M % q) % q for q in self.q]
         self.F = min(F, len(self.q))
         self.W = (self.r0 + 31) // 32
 
-    def split(self, b: int) -> int:
-        """Sorted slots [split, r0) wrap past M: the kernel's key + bucket search."""
-        thr = self.M - b
-        t32 = thr >> self.sh
-        s = self.BK[t32 >> self.bsh]
-        while self.K0[s] < t32:
-            s += 1
-        while self.K0[s] == t32 and s < self.r0 and self.S0[s] < thr:
-            s += 1
-        return s
+    def wrap_and_split(self, b2: int, d1: int) -> tuple[bool, int]:
+        """The kernel's ring-1 wrap and inner carry split from 32-bit keys (no 128-bit math on
+        the common path): A = M - b2 once per cycle; t = KA - K1[d1] (+ KM on a wrap) is the key
+        of thr = M - b to within +-1; slots keyed outside that band are decided by their keys,
+        the rest by exact comparison."""
+        M, sh = self.M, self.sh
+        A = M - b2
+        KA = A >> sh
+        k1 = self.K1[d1]
+        w1 = k1 > KA
+        t = self.KM - (k1 - KA) if w1 else KA - k1
+        assert 0 <= t <= 0xFFFFFFFF or k1 == KA
+        tl = max(t, 1) - 1
+        th = min(t, 0xFFFFFFFE) + 1
+        s = self.BK[tl >> self.bsh]
+        for _ in range(2):
+            if self.K0[s] < tl:
+                s += 1
+        if k1 == KA or self.K0[s] <= th:
+            self.exact_fallbacks += 1
+            w1 = self.terms[1][d1] >= A
+            b = b2 + self.terms[1][d1] - (M if w1 else 0)
+            thr = M - b
+            te = thr >> sh
+            s = self.BK[te >> self.bsh]
+            sent = self.S0 + [M]
+            while self.K0[s] < te:
+                s += 1
+            while self.K0[s] == te and sent[s] < thr:
+                s += 1
+        return w1, s
 
     def b2(self, c: int) -> int:
         rem, acc = c, 0
@@ -64,9 +88,9 @@ class KernelModel:
             b2 = self.b2(c)
             BQ2 = [(b2 % q + tc[f]) % q for f, q in enumerate(self.q[:self.F])]
             s1 = b2 + self.terms[1][d1]
-            w1 = s1 >= M
+            w1, sp = self.wrap_and_split(b2, d1)
+            assert w1 == (s1 >= M), "ring-1 wrap"
             b = s1 - M if w1 else s1
-            sp = self.split(b)
             assert sp == sum(1 for v in self.S0 if v + b < M), "carry split"
             for wd in range(self.W):
                 n_here = min(32, r0 - 32 * wd)
