@@ -171,13 +171,15 @@ struct SmemPlan {
 };
 
 // per-warp survivor queue (64 entries x 28 bytes), must match the kernel's EsQueue
-constexpr uint32_t kQueueBytes = 64u * 28u;
+constexpr uint32_t kQueueBytes = ES_QUEUE_BYTES;
 
 SmemPlan plan_smem(uint32_t small_max, uint32_t nf_max, const es_tune& tune, uint32_t fast_need) {
     SmemPlan p;
     const uint32_t warps = tune.threads / 32u;
     const uint32_t queues = kQueueBytes * warps;
-    const uint32_t counters = (uint32_t)align_up(4ull * nf_max * warps, 16);
+    // per-warp stage counters exist only in counting launches; shared memory is kept small so
+    // that the driver's carveout leaves the rest of the SM's 256 KB to L1 (the phase tables)
+    const uint32_t counters = tune.count_stages ? (uint32_t)align_up(4ull * nf_max * warps, 16) : 0u;
     const uint32_t fixed_tail = counters + queues;
     uint32_t budget = tune.smem_kb * 1024u;
     const uint32_t optin = (uint32_t)(g_dev.smem_optin - 1024);
@@ -348,15 +350,18 @@ int es_ctx_create(const es_plan_desc* d, const es_tune* tune_in, es_ctx** out) {
     const uint32_t bl = bitlen128(M);
     const uint32_t sh = bl > 32 ? bl - 32 : 0;
     const uint32_t kbits = bitlen128(M >> sh);
-    const uint32_t bsh = kbits > 10 ? kbits - 10 : 0;
+    const uint32_t bsh = kbits > ES_NBUCKET_LOG2 ? kbits - ES_NBUCKET_LOG2 : 0;
     std::vector<uint32_t> K0(r0);
     for (uint32_t i = 0; i < r0; ++i) K0[i] = (uint32_t)(S0[i] >> sh);
-    std::vector<uint16_t> BK(ES_NBUCKET + 1);
+    // bucket b: the first sorted slot whose key is >= b << bsh, and the keys of that slot and
+    // the next two (0xffffffff past the end), so that one 16-byte load settles the split
+    std::vector<uint32_t> BK(4ull * (ES_NBUCKET + 1));
     for (uint32_t bkt = 0; bkt <= ES_NBUCKET; ++bkt) {
         const uint64_t lim = (uint64_t)bkt << bsh;
         uint32_t n = 0;
         while (n < r0 && (uint64_t)K0[n] < lim) ++n;
-        BK[bkt] = (uint16_t)n;
+        BK[4 * bkt] = n;
+        for (uint32_t j = 0; j < 3; ++j) BK[4 * bkt + 1 + j] = n + j < r0 ? K0[n + j] : 0xffffffffu;
     }
 
     // ---- small block ----------------------------------------------------------------------
@@ -371,7 +376,7 @@ int es_ctx_create(const es_plan_desc* d, const es_tune* tune_in, es_ctx** out) {
     I.o_K0 = take(4ull * (r0 + 1));    // + sentinel K0[r0] = 0xffffffff
     I.o_I0 = take(4ull * r0);
     I.o_Q0 = take(4ull * ES_FMAX * r0);
-    I.o_BK = take(2ull * (ES_NBUCKET + 1));
+    I.o_BK = take(16ull * (ES_NBUCKET + 1));
     I.o_FC = take(sizeof(EsFilterC) * std::max<uint32_t>(nf, 1));
     I.o_K1 = take(4ull * r1);
     const size_t small_bytes = off;
@@ -402,7 +407,7 @@ int es_ctx_create(const es_plan_desc* d, const es_tune* tune_in, es_ctx** out) {
     }
     put128(I.o_S0, r0, M);             // stops the tie scan: M < thr never holds (thr <= M)
     put32(I.o_K0, r0, 0xffffffffu);    // stops the key scan: never < t32
-    memcpy(&small[I.o_BK], BK.data(), 2ull * (ES_NBUCKET + 1));
+    memcpy(&small[I.o_BK], BK.data(), 16ull * (ES_NBUCKET + 1));
     if (nf) memcpy(&small[I.o_FC], fc.data(), sizeof(EsFilterC) * nf);
 
     // ---- word-mask phase tables for the first FB filters ---------------------------------

@@ -10,8 +10,10 @@
 //                   S0[r0]      inner-ring terms sorted ascending            16 B each
 //                   K0[r0]      top-32-bit keys of S0 (carry-split search)    4 B each
 //                   I0[r0]      original inner digit of each sorted slot      4 B each
-//                   Q0[8][r0]   S0 mod q_f (scalar layout)                    4 B each
-//                   BK[1025]    carry-split bucket starts over key top bits   2 B each
+//                   Q0[8][r0]   S0 mod q_f (scalar layout, residue stage)     4 B each
+//                   BK[513]     carry-split buckets over the keys' top 9 bits:
+//                               first slot at or above the bucket, its key and
+//                               the next two keys                            16 B each
 //                   FC[nf]      per-filter constants (EsFilterC)             32 B each
 //   fast tables   for the first F_built filters: word-mask phase tables
 //                   P_f[phi][w] bit i = admissible((phi + S0[32w+i]) mod q_f), q_f x W words
@@ -21,7 +23,9 @@
 #include <stdint.h>
 
 #define ES_FMAX 8
-#define ES_NBUCKET 1024
+#define ES_NBUCKET_LOG2 9
+#define ES_NBUCKET (1u << ES_NBUCKET_LOG2)   // carry-split buckets over the 32-bit keys
+#define ES_QUEUE_BYTES 2304   // per-warp shared slot: entry queue, lane records, tail context
 #define ES_MAX_RINGS 64
 #define ES_MAX_FILTERS 192   // pi(1024) = 172 residual primes at most
 

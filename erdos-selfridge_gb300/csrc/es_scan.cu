@@ -22,13 +22,15 @@
 //    precomputed term residues and the wrap correction corr_f = -M mod q_f (the reference's v7
 //    identity, sieve/gpu_sieve_v9.py:9-18), reduced with unsigned min instead of branches.
 //  * Inner ring: its terms are sorted once on the host, so the wrap (s >= M) is a suffix of the
-//    sorted slots; its start (the carry split) comes from 32-bit keys through a 1024-bucket
+//    sorted slots; its start (the carry split) comes from 32-bit keys through a 512-bucket
 //    table.  Word-mask layout: a filter costs two table loads per 32 candidates,
 //    P_f[phase][w]; scalar layout: one residue + bit test per live candidate.  A warp leaves
 //    the cascade early when a ballot shows no live candidate.
-//  * Candidates passing the inner-ring stage are queued per warp and run through the exact
-//    remaining filters 32 at a time (full warps, not single lanes), from the 128-bit residue
-//    with limb weights and a Barrett reduction.
+//  * Inner words that still hold candidates after the inner-ring stage are queued per warp as
+//    one 16-byte entry per lane; a flush takes 32 entries, one candidate per lane (full warps,
+//    not single lanes), runs the next filters from 32-bit term residues, and gives only the
+//    few candidates left the exact tail: n mod M rebuilt in 128 bits, then limb weights and a
+//    Barrett reduction per filter.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -139,14 +141,47 @@ __device__ __forceinline__ void copy_words(uint32_t* dst, const uint32_t* __rest
     for (uint32_t i = (n4 << 2) + threadIdx.x; i < nwords; i += blockDim.x) dst[i] = __ldg(src + i);
 }
 
-// Per-warp queue of candidates that passed the inner-ring stage; the exact cascade tail runs
-// on 32 queued candidates at a time so that whole warps, not single lanes, do the 128-bit work.
-#define ES_QCAP 64
-struct EsQueue {
-    uint4 b2[ES_QCAP];                 // sum of the ring >= 2 terms mod M (32-bit limbs)
-    unsigned long long oidx[ES_QCAP];  // outer index
-    uint32_t info[ES_QCAP];            // sorted inner slot | ring-1 digit << 16
+// Everything the flush, the cascade tail and the emit need for one warp-unit.  It lives in the
+// warp's slot in shared memory, written once per warp-unit and read only on the flush path, so
+// none of it occupies registers across the ring-1 sweep.
+struct TailCtx {
+    U4 M;
+    uint64_t M_lo;
+    uint64_t t_blk;
+    uint64_t e_base;                   // strip entry of lane 0 (ring-1 cycle or list position)
+    const unsigned long long* list;    // outer-index list of the item, or null (a range)
+    const uint4* sT1;                  // ring-1 terms (shared)
+    const uint4* sS0;                  // sorted inner-ring terms (shared)
+    const uint32_t* sI0;               // original inner digit of each sorted slot (shared)
+    const uint32_t* sTQ1;              // ring-1 term residues, ES_FMAX per digit (shared)
+    const uint32_t* sQ0;               // sorted inner-ring term residues, r0 per filter (shared)
+    const EsFilterC* sFC;
+    const uint32_t* tc;
+    const uint32_t* allowed_g;
+    es_survivor* surv;
+    unsigned long long* surv_n;
+    unsigned long long* group_found;
+    uint64_t surv_cap;
+    uint32_t kp1, Feff, FR, nf, wcnt_saddr, item_id, group, r0, r1, strip;
+    bool M_big;
 };
+
+// Per-warp queue of inner-word pairs that still hold candidates after the inner-ring stage.  An
+// entry is one lane's words w, w+1 of one outer index: {candidate bits of word w, of word w+1,
+// d1 | carry split << 16, lane | ring-1 wrap << 5 | w << 6}.
+// The lane's ring-1 cycle is described once per strip step by its record (b2 and the residues
+// of b2 for the residue-stage filters), so a push is one 16-byte store per lane; the queue is
+// drained before the records change.  The flush runs 32 entries at a time (whole warps): first
+// the next ES_NRES filters from 32-bit residues (the tables of the inner-ring stage carry them),
+// then, for the few candidates left, n mod M and the exact tail.
+#define ES_QCAP 64
+#define ES_NRES 4
+struct EsQueue {
+    uint4 ent[ES_QCAP];
+    uint4 rec[32][2];                  // per lane: b2 (limbs); residues of b2 + block term
+    TailCtx ctx;                       // the warp's current item (see TailCtx)
+};
+static_assert(sizeof(EsQueue) <= ES_QUEUE_BYTES, "per-warp slot overflows its shared-memory share");
 
 __device__ __forceinline__ void red_add_shared(uint32_t saddr, uint32_t v) {
     // Not visible to the compiler as a store: the counters are read only after a __syncwarp.
@@ -173,40 +208,10 @@ __device__ __forceinline__ void row8(const uint4* row, uint32_t (&v)[8]) {
     }
 }
 
-// Everything the cascade tail and the emit need for one item, passed by value into the
-// force-inlined helpers below (nothing escapes to local memory).
-struct TailCtx {
-    U4 M;
-    uint64_t M_lo;
-    uint64_t t_blk;
-    const uint4* sT1;          // ring-1 terms (shared)
-    const uint4* sS0;          // sorted inner-ring terms (shared)
-    const uint32_t* sI0;       // original inner digit of each sorted slot (shared)
-    const EsFilterC* sFC;
-    const uint32_t* tc;
-    const uint32_t* allowed_g;
-    es_survivor* surv;
-    unsigned long long* surv_n;
-    unsigned long long* group_found;
-    uint64_t surv_cap;
-    uint32_t kp1, Feff, nf, wcnt_saddr, item_id, group, r0;
-    bool M_big;
-};
-
-// n mod M and the position index of queued candidate (b2, oidx, slot, d1)
-__device__ __forceinline__ void rebuild(const TailCtx& C, const U4 b2, uint64_t oidx, uint32_t info,
-                                        U4& s, uint64_t& idx) {
-    const uint32_t slot = info & 0xffffu, d1 = info >> 16;
-    uint32_t wm;
-    const U4 b = addmod(b2, u4(C.sT1[d1]), C.M, wm);
-    s = addmod(b, u4(C.sS0[slot]), C.M, wm);
-    idx = oidx * (uint64_t)C.r0 + C.sI0[slot];
-}
-
-// exact tail of the cascade for one candidate (filters Feff..nf-1), then the emit
+// exact tail of the cascade for one candidate (filters f0..nf-1), then the emit
 template <bool COUNT>
-__device__ __forceinline__ void tail_one(const TailCtx& C, const U4 s, uint64_t idx) {
-    for (uint32_t f = C.Feff; f < C.nf; ++f) {
+__device__ __forceinline__ void tail_one(const TailCtx& C, uint32_t f0, const U4 s, uint64_t idx) {
+    for (uint32_t f = f0; f < C.nf; ++f) {
         const EsFilterC fc = C.sFC[f];
         uint32_t r = mod128(s, fc) + C.tc[f];
         if (r >= fc.q) r -= fc.q;
@@ -234,73 +239,78 @@ __device__ __forceinline__ void tail_one(const TailCtx& C, const U4 s, uint64_t 
     if (good && C.group_found) atomicMin(C.group_found + C.group, (unsigned long long)C.t_blk);
 }
 
-// warp-uniform: run the tail on up to 32 queued candidates
+// warp-uniform: one pass over up to 32 queued entries.  Each lane takes the lowest candidate of
+// its entry (the rest of the entry goes back on the queue), so the residue stage runs converged
+// and the warp leaves it as soon as no lane has a live candidate; the few candidates left take
+// n mod M and the exact tail.
 template <bool COUNT>
-__device__ __forceinline__ void flush(const TailCtx& C, EsQueue* Q, uint32_t lane, uint32_t& qhead,
+__device__ __forceinline__ void flush(EsQueue* Q, uint32_t lane, uint32_t step, uint32_t& qhead,
                                       uint32_t& qsize) {
     __syncwarp();
+    const TailCtx& C = Q->ctx;
     const uint32_t n = qsize < 32u ? qsize : 32u;
-    if (lane < n) {
-        const uint32_t e = (qhead + lane) & (ES_QCAP - 1);
-        U4 s;
-        uint64_t idx;
-        rebuild(C, u4(Q->b2[e]), Q->oidx[e], Q->info[e], s, idx);
-        tail_one<COUNT>(C, s, idx);
-    }
+    const uint4 en = Q->ent[(qhead + lane) & (ES_QCAP - 1)];
+    const uint64_t bits = lane < n ? ((uint64_t)en.y << 32) | en.x : 0ull;
+    const uint64_t rest = bits & (bits - 1ull);
+    const uint32_t back = __ballot_sync(0xffffffffu, rest != 0u);
+    __syncwarp();   // every lane holds its entry before any slot is reused
     qhead = (qhead + n) & (ES_QCAP - 1);
     qsize -= n;
+    if (rest) {
+        // lands on a free or just-consumed slot: qsize - n + popc(back) <= old qsize < ES_QCAP
+        const uint32_t pos = (qhead + qsize + __popc(back & ((1u << lane) - 1u))) & (ES_QCAP - 1);
+        Q->ent[pos] = make_uint4((uint32_t)rest, (uint32_t)(rest >> 32), en.z, en.w);
+    }
+    qsize += __popc(back);
+    const bool has = bits != 0ull;
+    const uint32_t i = has ? __ffsll((long long)bits) - 1u : 0u;
+    const uint32_t d1 = has ? (en.z & 0xffffu) : 0u;
+    const uint32_t slot = has ? ((en.w >> 6) << 5) + i : 0u;
+    const uint32_t own = has ? (en.w & 31u) : 0u;
+    const bool wrap1 = has && ((en.w >> 5) & 1u);
+    const bool cw = has && slot >= (en.z >> 16);   // sorted slots from the split on wrap past M
+    const uint4 bq = Q->rec[own][1];
+    const uint32_t bqv[ES_NRES] = {bq.x, bq.y, bq.z, bq.w};
+    const uint32_t f0 = C.Feff, fr = C.FR, r0 = C.r0;
+    bool ok = has;
+#pragma unroll
+    for (uint32_t j = 0; j < ES_NRES; ++j) {
+        const uint32_t f = f0 + j;
+        if (f < fr && __any_sync(0xffffffffu, ok)) {
+            const EsFilterC& fc = C.sFC[f];
+            const uint32_t q = fc.q, corr = fc.corr;
+            // n mod q_f = b2 + T1[d1] + S0[slot] mod q_f, with -M mod q_f per wrap
+            uint32_t x = red2(bqv[j] + C.sTQ1[d1 * ES_FMAX + f] + (wrap1 ? corr : 0u), q);
+            x = red2(x + C.sQ0[f * r0 + slot] + (cw ? corr : 0u), q);
+            const uint32_t wv = __ldg(C.allowed_g + fc.off + (x >> 5));
+            ok = ok && ((wv >> (x & 31u)) & 1u);
+            if (COUNT && ok) red_add_shared(C.wcnt_saddr + 4u * f, 1u);
+        }
+    }
+    if (ok) {
+        uint32_t wm;
+        const U4 b = addmod(u4(Q->rec[own][0]), u4(C.sT1[d1]), C.M, wm);
+        const U4 s = addmod(b, u4(C.sS0[slot]), C.M, wm);
+        const uint64_t e = C.e_base + (uint64_t)own * C.strip + step;
+        const uint64_t oidx = C.list ? __ldg(C.list + e) : e * C.r1 + d1;
+        tail_one<COUNT>(C, fr, s, oidx * (uint64_t)r0 + C.sI0[slot]);
+    }
     __syncwarp();
 }
 
-// warp-uniform: queue the set bits of one inner word (sorted slots base + i) of outer index
-// oidx = c * r1 + d1; only (b2, oidx, slot, d1) are stored, n mod M is rebuilt at the flush
+// warp-uniform (has = ballot of (lo | hi) != 0, nonzero; qsize < 32 on entry): queue the word
+// pair (wd, wd + 1) of every lane that has candidates, then flush while 32 entries are waiting
 template <bool COUNT>
-__device__ __forceinline__ void push(const TailCtx& C, EsQueue* Q, uint32_t lane, uint32_t& qhead,
-                                     uint32_t& qsize, uint32_t bits, uint32_t base, const U4 b2,
-                                     uint64_t oidx, uint32_t d1) {
-    const uint32_t n = __popc(bits);
-    uint32_t excl, tot;
-    if (__ballot_sync(0xffffffffu, n > 1u) == 0u) {
-        // common case: at most one candidate per lane
-        const uint32_t has = __ballot_sync(0xffffffffu, n != 0u);
-        excl = __popc(has & ((1u << lane) - 1u));
-        tot = __popc(has);
-    } else {
-        uint32_t incl = n;
-#pragma unroll
-        for (uint32_t o = 1; o < 32; o <<= 1) {
-            const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += v;
-        }
-        excl = incl - n;
-        tot = __shfl_sync(0xffffffffu, incl, 31);
+__device__ __forceinline__ void push(EsQueue* Q, uint32_t lane, uint32_t step, uint32_t& qhead,
+                                     uint32_t& qsize, uint32_t has, uint32_t lo, uint32_t hi,
+                                     uint32_t split, uint32_t d1, uint32_t wd, uint32_t wm1) {
+    if (lo | hi) {
+        const uint32_t pos = (qhead + qsize + __popc(has & ((1u << lane) - 1u))) & (ES_QCAP - 1);
+        Q->ent[pos] = make_uint4(lo, hi, d1 | (split << 16), lane | (wm1 & 32u) | (wd << 6));
     }
-    if (qsize + tot > ES_QCAP)
-        while (qsize) flush<COUNT>(C, Q, lane, qhead, qsize);
-    if (tot > ES_QCAP) {
-        // survivor-dense plans (tiny k): tail in place
-        while (bits) {
-            const uint32_t i = __ffs(bits) - 1u;
-            bits &= bits - 1u;
-            U4 s;
-            uint64_t idx;
-            rebuild(C, b2, oidx, (base + i) | (d1 << 16), s, idx);
-            tail_one<COUNT>(C, s, idx);
-        }
-        return;
-    }
-    uint32_t pos = qhead + qsize + excl;
-    while (bits) {
-        const uint32_t i = __ffs(bits) - 1u;
-        bits &= bits - 1u;
-        const uint32_t qe = pos & (ES_QCAP - 1);
-        Q->b2[qe] = make_uint4(b2.x, b2.y, b2.z, b2.w);
-        Q->oidx[qe] = oidx;
-        Q->info[qe] = (base + i) | (d1 << 16);
-        ++pos;
-    }
-    qsize += tot;
-    while (qsize >= 32u) flush<COUNT>(C, Q, lane, qhead, qsize);
+    qsize += __popc(has);
+    // each pass retires one candidate per lane, so this ends
+    while (qsize >= 32u) flush<COUNT>(Q, lane, step, qhead, qsize);
 }
 
 // Warp-uniform: scan one warp-unit w of `item`, whose plan is staged in smem / si.
@@ -309,28 +319,10 @@ __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, u
                                           EsQueue* Q, uint32_t* wcnt,
                                           uint32_t wcnt_saddr, uint32_t lane, unsigned long long w,
                                           const EsItem& item, uint32_t item_id) {
-    TailCtx C;
-    C.M = U4{(uint32_t)si.M_lo, (uint32_t)(si.M_lo >> 32), (uint32_t)si.M_hi, (uint32_t)(si.M_hi >> 32)};
-    C.M_lo = si.M_lo;
-    C.kp1 = si.k + 1u;
-    C.M_big = (si.M_hi != 0) || (si.M_lo > C.kp1);
-    C.nf = si.n_filters;
-    C.r0 = si.r0;
-    C.sT1 = reinterpret_cast<const uint4*>(smem + si.o_T1);
-    C.sS0 = reinterpret_cast<const uint4*>(smem + si.o_S0);
-    C.sI0 = reinterpret_cast<const uint32_t*>(smem + si.o_I0);
-    C.sFC = reinterpret_cast<const EsFilterC*>(smem + si.o_FC);
-    C.tc = L.items ? item.tconst : L.tconst0;
-    C.allowed_g = si.allowed;
-    C.surv = L.surv;
-    C.surv_n = L.surv_n;
-    C.group_found = L.group_found;
-    C.surv_cap = L.surv_cap;
-    C.wcnt_saddr = wcnt_saddr;
-    C.item_id = item_id;
-    C.group = item.group;
-    C.t_blk = item.t;
-    const U4 M = C.M;
+    const U4 M{(uint32_t)si.M_lo, (uint32_t)(si.M_lo >> 32), (uint32_t)si.M_hi, (uint32_t)(si.M_hi >> 32)};
+    const EsFilterC* sFC = reinterpret_cast<const EsFilterC*>(smem + si.o_FC);
+    const uint32_t* tcv = L.items ? item.tconst : L.tconst0;
+    const uint32_t nf = si.n_filters;
     const uint32_t r0 = si.r0, r1 = si.r1, r2 = si.r2;
     const uint32_t Wn = WT ? (uint32_t)WT : si.W;
     const uint32_t bsh = si.bsh, tail = si.tail_mask;
@@ -340,11 +332,12 @@ __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, u
     const uint4* sTQ1 = reinterpret_cast<const uint4*>(smem + si.o_TQ1);
     const uint4* sD2 = reinterpret_cast<const uint4*>(smem + si.o_D2);
     const uint4* sDQ2 = reinterpret_cast<const uint4*>(smem + si.o_DQ2);
+    const uint32_t* sDQ2w = reinterpret_cast<const uint32_t*>(sDQ2);
     const uint4* sS0 = reinterpret_cast<const uint4*>(smem + si.o_S0);
     const uint32_t* sK0 = reinterpret_cast<const uint32_t*>(smem + si.o_K0);
     const uint32_t* sI0 = reinterpret_cast<const uint32_t*>(smem + si.o_I0);
     const uint32_t* sQ0 = reinterpret_cast<const uint32_t*>(smem + si.o_Q0);
-    const uint16_t* sBK = reinterpret_cast<const uint16_t*>(smem + si.o_BK);
+    const uint4* sBK = reinterpret_cast<const uint4*>(smem + si.o_BK);   // {slot, 3 keys}
     const uint32_t* sK1 = reinterpret_cast<const uint32_t*>(smem + si.o_K1);
     const uint32_t KM = si.km;
     const uint64_t ob = item.o_begin, oe = item.o_end;
@@ -354,18 +347,51 @@ __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, u
     uint32_t Feff = (uint32_t)F;
     if (LAYOUT != ES_LAYOUT_WORDMASK) {
         if (Feff > L.mask_filters) Feff = L.mask_filters;
-        if (Feff > C.nf) Feff = C.nf;
+        if (Feff > nf) Feff = nf;
     }
-    C.Feff = Feff;
+    // residue stage: the next ES_NRES filters that carry 32-bit term residues
+    const uint32_t FR = min(si.F_built, Feff + ES_NRES) > Feff ? min(si.F_built, Feff + ES_NRES) : Feff;
+    TailCtx& C = Q->ctx;
+    if (lane == 0) {
+        C.M = M;
+        C.M_lo = si.M_lo;
+        C.kp1 = si.k + 1u;
+        C.M_big = (si.M_hi != 0) || (si.M_lo > C.kp1);
+        C.nf = nf;
+        C.r0 = si.r0;
+        C.sT1 = reinterpret_cast<const uint4*>(smem + si.o_T1);
+        C.sS0 = reinterpret_cast<const uint4*>(smem + si.o_S0);
+        C.sI0 = reinterpret_cast<const uint32_t*>(smem + si.o_I0);
+        C.sTQ1 = reinterpret_cast<const uint32_t*>(smem + si.o_TQ1);
+        C.sQ0 = reinterpret_cast<const uint32_t*>(smem + si.o_Q0);
+        C.sFC = sFC;
+        C.tc = tcv;
+        C.allowed_g = si.allowed;
+        C.surv = L.surv;
+        C.surv_n = L.surv_n;
+        C.group_found = L.group_found;
+        C.surv_cap = L.surv_cap;
+        C.wcnt_saddr = wcnt_saddr;
+        C.item_id = item_id;
+        C.group = item.group;
+        C.t_blk = item.t;
+        C.Feff = Feff;
+        C.FR = FR;
+        C.r1 = si.r1;
+        C.strip = L.strip;
+        C.list = reinterpret_cast<const unsigned long long*>(item.list);
+        C.e_base = (item.list ? item.o_begin : item.c_begin) + (w - item.unit_begin) * 32ull * L.strip;
+    }
+    __syncwarp();
     constexpr int FA = F > 0 ? F : 1;   // array extent
     uint32_t qf[FA], corr[FA];
     const uint32_t* tab[FA];
 #pragma unroll
     for (int f = 0; f < F; ++f) {
         const bool on = (uint32_t)f < Feff;
-        qf[f] = on ? C.sFC[f].q : 1u;
-        corr[f] = on ? C.sFC[f].corr : 0u;
-        tab[f] = LAYOUT == ES_LAYOUT_WORDMASK ? masks_g + si.mask_off[f] : C.allowed_g + (on ? C.sFC[f].off : 0u);
+        qf[f] = on ? sFC[f].q : 1u;
+        corr[f] = on ? sFC[f].corr : 0u;
+        tab[f] = LAYOUT == ES_LAYOUT_WORDMASK ? masks_g + si.mask_off[f] : si.allowed + (on ? sFC[f].off : 0u);
     }
     uint32_t cnt[FA];
 #pragma unroll
@@ -418,13 +444,31 @@ __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, u
                 row8<F>(sDQ2 + d2 * (ES_FMAX / 4), dq);
 #pragma unroll
                 for (int f = 0; f < F; ++f) BQ2[f] = red2(BQ2[f] + dq[f] + (corr[f] & wm), qf[f]);
+                // this lane's record: b2 and the residue-stage residues, stepped the same way
+                const uint4 rq = Q->rec[lane][1];
+                uint32_t rv[ES_NRES] = {rq.x, rq.y, rq.z, rq.w};
+#pragma unroll
+                for (uint32_t j = 0; j < ES_NRES; ++j) {
+                    const uint32_t f = Feff + j;
+                    if (f < FR) rv[j] = red2(rv[j] + sDQ2w[d2 * ES_FMAX + f] + (sFC[f].corr & wm), sFC[f].q);
+                }
+                Q->rec[lane][0] = make_uint4(b2.x, b2.y, b2.z, b2.w);
+                Q->rec[lane][1] = make_uint4(rv[0], rv[1], rv[2], rv[3]);
                 ++d2;
             } else if (!(have && c == prev_c)) {
                 b2 = decode_cycle(si, c, M, d2);
 #pragma unroll
                 for (int f = 0; f < F; ++f) {
-                    if ((uint32_t)f < Feff) BQ2[f] = red1(mod128(b2, C.sFC[f]) + C.tc[f], qf[f]);
+                    if ((uint32_t)f < Feff) BQ2[f] = red1(mod128(b2, sFC[f]) + tcv[f], qf[f]);
                 }
+                uint32_t rv[ES_NRES] = {0u, 0u, 0u, 0u};
+#pragma unroll
+                for (uint32_t j = 0; j < ES_NRES; ++j) {
+                    const uint32_t f = Feff + j;
+                    if (f < FR) rv[j] = red1(mod128(b2, sFC[f]) + tcv[f], sFC[f].q);
+                }
+                Q->rec[lane][0] = make_uint4(b2.x, b2.y, b2.z, b2.w);
+                Q->rec[lane][1] = make_uint4(rv[0], rv[1], rv[2], rv[3]);
                 have = true;
             }
             prev_c = c;
@@ -449,11 +493,14 @@ __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, u
             const uint32_t t = wm1 ? KM - (k1 - KA) : KA - k1;
             const uint32_t tl = max(t, 1u) - 1u;
             const uint32_t th = min(t, 0xfffffffeu) + 1u;
-            uint32_t split = sBK[tl >> bsh];
-            split += (sK0[split] < tl) ? 1u : 0u;
-            split += (sK0[split] < tl) ? 1u : 0u;
+            // the bucket of tl holds its first slot and the next three keys (sorted): the split
+            // is that slot plus the keys below tl among the first two
+            const uint4 bk = sBK[tl >> bsh];
+            const bool s1 = bk.y < tl, s2 = bk.z < tl;
+            uint32_t split = bk.x + (s1 ? 1u : 0u) + (s2 ? 1u : 0u);
+            const uint32_t ks = s2 ? bk.w : (s1 ? bk.z : bk.y);   // key of slot `split`
             // rare: a key tie with A, a key inside the +-1 band, or a crowded bucket -> exact
-            const bool rare = (k1 == KA) || (sK0[split] <= th);
+            const bool rare = (k1 == KA) || (ks <= th);
             if (__any_sync(0xffffffffu, rare)) {
                 if (rare) {
                     uint32_t wx, brw;
@@ -462,12 +509,13 @@ __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, u
                     const U4 thr = sub128(M, b, brw);
                     const uint32_t te = __funnelshift_r(kl == 0 ? thr.x : (kl == 1 ? thr.y : thr.z),
                                                         kl == 0 ? thr.y : (kl == 1 ? thr.z : thr.w), ko);
-                    split = sBK[te >> bsh];
+                    split = sBK[te >> bsh].x;
                     while (sK0[split] < te) ++split;
                     while (sK0[split] == te && lt128(u4(sS0[split]), thr)) ++split;   // S0[r0] = M stops it
                 }
             }
 
+            uint32_t lo = 0u;   // bits of an even word, queued with the odd word after it
             for (uint32_t wd = 0; wd < Wn; ++wd) {
                 const uint32_t valid = (wd + 1u == Wn) ? tail : 0xffffffffu;
                 uint32_t bits = act ? valid : 0u;
@@ -507,12 +555,19 @@ __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, u
                     }
                 }
                 // ---- queue the survivors of the inner-ring stage -----------------------------
-                if (__ballot_sync(0xffffffffu, bits != 0u))
-                    push<COUNT>(C, Q, lane, qhead, qsize, bits, base, b2, c * r1 + d1, d1);
+                if ((wd & 1u) == 0u && wd + 1u < Wn) {
+                    lo = bits;
+                    continue;
+                }
+                const bool odd = (wd & 1u) != 0u;
+                const uint32_t plo = odd ? lo : bits, phi = odd ? bits : 0u;
+                const uint32_t has = __ballot_sync(0xffffffffu, (plo | phi) != 0u);
+                if (has) push<COUNT>(Q, lane, step, qhead, qsize, has, plo, phi, split, d1, wd & ~1u, wm1);
             }
         }
+        // the records change with the next strip step: drain the queue
+        while (qsize) flush<COUNT>(Q, lane, step, qhead, qsize);
     }
-    while (qsize) flush<COUNT>(C, Q, lane, qhead, qsize);
     // ---- per-stage counts of this warp-unit into the item's totals ----------------------
     if (COUNT) {
         unsigned long long* gc = item.counts;
@@ -522,7 +577,7 @@ __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, u
             if (lane == 0 && v && gc && (uint32_t)f < Feff) atomicAdd(gc + f, (unsigned long long)v);
         }
         __syncwarp();
-        for (uint32_t f = Feff + lane; f < C.nf; f += 32u) {
+        for (uint32_t f = Feff + lane; f < nf; f += 32u) {
             const uint32_t v = wcnt[f];
             if (v) {
                 if (gc) atomicAdd(gc + f, (unsigned long long)v);
@@ -554,7 +609,7 @@ __global__ void __launch_bounds__(ES_LB_THREADS, ES_LB_MINB) es_scan_kernel(cons
     const uint32_t tid = threadIdx.x;
     const uint32_t lane = tid & 31u;
     const uint32_t warp = tid >> 5;
-    EsQueue* Q = reinterpret_cast<EsQueue*>(smem + L.queue_off) + warp;
+    EsQueue* Q = reinterpret_cast<EsQueue*>(smem + L.queue_off + warp * ES_QUEUE_BYTES);
     uint32_t* wcnt = reinterpret_cast<uint32_t*>(smem + L.cnt_off) + warp * L.nf_max;
     const uint32_t wcnt_saddr = (uint32_t)__cvta_generic_to_shared(wcnt);
     const EsItem* items = L.items ? L.items : &L.item0;

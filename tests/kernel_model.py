@@ -3,7 +3,8 @@
 Re-derives, in plain Python integers, every table the device uses (sorted inner ring, 32-bit
 carry-split keys and buckets, ring-1 residues, word-mask phases, wrap corrections) and walks
 positions exactly the way es_scan_kernel does: b2 from rings >= 2, one ring-1 term, the carry
-split of the inner ring, the word-mask stage over the first F filters, then the exact tail.
+split of the inner ring, the word-mask stage over the first F filters, the residue stage over
+the next four, then the exact tail.
 It isolates "the decomposition is wrong" from "the CUDA is wrong", like the reference's CPU
 emulation of its kernel index scheme (tests/test_enumeration.py).
 """
@@ -27,8 +28,11 @@ class KernelModel:
         self.sh = bl - 32 if bl > 32 else 0
         self.K0 = [v >> self.sh for v in self.S0] + [0xFFFFFFFF]      # sentinel
         kb = (M >> self.sh).bit_length()
-        self.bsh = kb - 10 if kb > 10 else 0
-        self.BK = [sum(1 for x in self.K0[:-1] if x < (b << self.bsh)) for b in range(1025)]
+        self.bsh = kb - 9 if kb > 9 else 0                  # 512 buckets
+        self.BK = [sum(1 for x in self.K0[:-1] if x < (b << self.bsh)) for b in range(513)]
+        # the device's 16-byte bucket entry: first slot and the keys of it and the next two
+        pad = self.K0 + [0xFFFFFFFF] * 2
+        self.BKX = [(n, pad[n], pad[n + 1], pad[n + 2]) for n in self.BK]
         self.K1 = [v >> self.sh for v in terms[1]]       # 32-bit keys of the ring-1 terms
         self.KM = M >> self.sh
         self.exact_fallbacks = 0
@@ -36,6 +40,8 @@ class KernelModel:
         self.ok = [set(plan.info[p][1]) for p in plan.rest]
         self.corr = [(q - M % q) % q for q in self.q]
         self.F = min(F, len(self.q))
+        # filters of the residue stage: the next four that carry 32-bit term residues
+        self.FR = max(self.F, min(8, len(self.q), self.F + 4))
         self.W = (self.r0 + 31) // 32
 
     def wrap_and_split(self, b2: int, d1: int) -> tuple[bool, int]:
@@ -52,11 +58,11 @@ class KernelModel:
         assert 0 <= t <= 0xFFFFFFFF or k1 == KA
         tl = max(t, 1) - 1
         th = min(t, 0xFFFFFFFE) + 1
-        s = self.BK[tl >> self.bsh]
-        for _ in range(2):
-            if self.K0[s] < tl:
-                s += 1
-        if k1 == KA or self.K0[s] <= th:
+        n, ka, kb, kc = self.BKX[tl >> self.bsh]
+        s = n + (ka < tl) + (kb < tl)
+        ks = kc if kb < tl else (kb if ka < tl else ka)
+        assert ks == self.K0[s]
+        if k1 == KA or ks <= th:
             self.exact_fallbacks += 1
             w1 = self.terms[1][d1] >= A
             b = b2 + self.terms[1][d1] - (M if w1 else 0)
@@ -87,6 +93,7 @@ class KernelModel:
             c, d1 = divmod(int(oidx), self.r1)
             b2 = self.b2(c)
             BQ2 = [(b2 % q + tc[f]) % q for f, q in enumerate(self.q[:self.F])]
+            BQx = {f: (b2 % self.q[f] + tc[f]) % self.q[f] for f in range(self.F, self.FR)}
             s1 = b2 + self.terms[1][d1]
             w1, sp = self.wrap_and_split(b2, d1)
             assert w1 == (s1 >= M), "ring-1 wrap"
@@ -109,8 +116,26 @@ class KernelModel:
                         continue
                     slot = 32 * wd + i
                     s = (b + self.S0[slot]) % M
+                    cw = (cm >> i) & 1
                     ok = True
-                    for f in range(self.F, nf):
+                    # residue stage (the flush): 32-bit residues of b2, the ring-1 term and the
+                    # inner term, with -M mod q per wrap; each sum stays below 3q
+                    for f in range(self.F, self.FR):
+                        q, corr = self.q[f], self.corr[f]
+                        x = BQx[f] + self.terms[1][d1] % q + (corr if w1 else 0)
+                        assert x < 3 * q
+                        x %= q
+                        x = x + self.S0[slot] % q + (corr if cw else 0)
+                        assert x < 3 * q
+                        x %= q
+                        assert x == (s % q + tc[f]) % q, "residue stage"
+                        if x not in self.ok[f]:
+                            ok = False
+                            break
+                        counts[f] += 1
+                    if not ok:
+                        continue
+                    for f in range(self.FR, nf):
                         if (s % self.q[f] + tc[f]) % self.q[f] not in self.ok[f]:
                             ok = False
                             break
