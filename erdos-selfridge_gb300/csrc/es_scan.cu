@@ -107,6 +107,29 @@ __device__ __forceinline__ uint32_t red1(uint32_t v, uint32_t q) { return min(v,
 // v mod q for v < 3q
 __device__ __forceinline__ uint32_t red2(uint32_t v, uint32_t q) { return red1(red1(v, q), q); }
 
+// Volatile shared loads: values the ring-1 sweep needs only on its rare paths are re-read where
+// they are used instead of being held in registers across the sweep.
+__device__ __forceinline__ uint32_t ldv32(const void* p) {
+    uint32_t v;
+    asm volatile("ld.volatile.shared.u32 %0, [%1];" : "=r"(v) : "r"((uint32_t)__cvta_generic_to_shared(p)));
+    return v;
+}
+__device__ __forceinline__ U4 ldv128(const void* p) {
+    U4 v;
+    asm volatile("ld.volatile.shared.v4.u32 {%0, %1, %2, %3}, [%4];"
+                 : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+                 : "r"((uint32_t)__cvta_generic_to_shared(p)));
+    return v;
+}
+__device__ __forceinline__ U4 ldv_M(const EsInst& si) {   // M_lo, M_hi are adjacent
+    return ldv128(&si.M_lo);
+}
+// 32 bits of x from bit sh (sh < 96): the carry-split key
+__device__ __forceinline__ uint32_t key32(const U4 x, uint32_t sh) {
+    const uint32_t kl = sh >> 5, ko = sh & 31u;
+    return __funnelshift_r(kl == 0 ? x.x : (kl == 1 ? x.y : x.z), kl == 0 ? x.y : (kl == 1 ? x.z : x.w), ko);
+}
+
 // b2 = sum_{j>=2} term_j[d_j] mod M for ring-1 cycle c; also returns the ring-2 digit.
 __device__ __noinline__ U4 decode_cycle(const EsInst& I, uint64_t c, const U4 M, uint32_t& d2) {
     uint64_t rem = c;
@@ -150,12 +173,6 @@ struct TailCtx {
     uint64_t t_blk;
     uint64_t e_base;                   // strip entry of lane 0 (ring-1 cycle or list position)
     const unsigned long long* list;    // outer-index list of the item, or null (a range)
-    const uint4* sT1;                  // ring-1 terms (shared)
-    const uint4* sS0;                  // sorted inner-ring terms (shared)
-    const uint32_t* sI0;               // original inner digit of each sorted slot (shared)
-    const uint32_t* sTQ1;              // ring-1 term residues, ES_FMAX per digit (shared)
-    const uint32_t* sQ0;               // sorted inner-ring term residues, r0 per filter (shared)
-    const EsFilterC* sFC;
     const uint32_t* tc;
     const uint32_t* allowed_g;
     es_survivor* surv;
@@ -210,9 +227,10 @@ __device__ __forceinline__ void row8(const uint4* row, uint32_t (&v)[8]) {
 
 // exact tail of the cascade for one candidate (filters f0..nf-1), then the emit
 template <bool COUNT>
-__device__ __forceinline__ void tail_one(const TailCtx& C, uint32_t f0, const U4 s, uint64_t idx) {
+__device__ __forceinline__ void tail_one(const TailCtx& C, const EsFilterC* sFC, uint32_t f0, const U4 s,
+                                         uint64_t idx) {
     for (uint32_t f = f0; f < C.nf; ++f) {
-        const EsFilterC fc = C.sFC[f];
+        const EsFilterC fc = sFC[f];
         uint32_t r = mod128(s, fc) + C.tc[f];
         if (r >= fc.q) r -= fc.q;
         const uint32_t wv = __ldg(C.allowed_g + fc.off + (r >> 5));
@@ -244,10 +262,16 @@ __device__ __forceinline__ void tail_one(const TailCtx& C, uint32_t f0, const U4
 // and the warp leaves it as soon as no lane has a live candidate; the few candidates left take
 // n mod M and the exact tail.
 template <bool COUNT>
-__device__ __forceinline__ void flush(EsQueue* Q, uint32_t lane, uint32_t step, uint32_t& qhead,
-                                      uint32_t& qsize) {
+__device__ __forceinline__ void flush(EsQueue* Q, const unsigned char* smem, const EsInst& si, uint32_t lane,
+                                      uint32_t step, uint32_t& qhead, uint32_t& qsize) {
     __syncwarp();
     const TailCtx& C = Q->ctx;
+    const uint4* sT1 = reinterpret_cast<const uint4*>(smem + si.o_T1);
+    const uint4* sS0 = reinterpret_cast<const uint4*>(smem + si.o_S0);
+    const uint32_t* sI0 = reinterpret_cast<const uint32_t*>(smem + si.o_I0);
+    const uint32_t* sTQ1 = reinterpret_cast<const uint32_t*>(smem + si.o_TQ1);
+    const uint32_t* sQ0 = reinterpret_cast<const uint32_t*>(smem + si.o_Q0);
+    const EsFilterC* sFC = reinterpret_cast<const EsFilterC*>(smem + si.o_FC);
     const uint32_t n = qsize < 32u ? qsize : 32u;
     const uint4 en = Q->ent[(qhead + lane) & (ES_QCAP - 1)];
     const uint64_t bits = lane < n ? ((uint64_t)en.y << 32) | en.x : 0ull;
@@ -277,11 +301,11 @@ __device__ __forceinline__ void flush(EsQueue* Q, uint32_t lane, uint32_t step, 
     for (uint32_t j = 0; j < ES_NRES; ++j) {
         const uint32_t f = f0 + j;
         if (f < fr && __any_sync(0xffffffffu, ok)) {
-            const EsFilterC& fc = C.sFC[f];
+            const EsFilterC& fc = sFC[f];
             const uint32_t q = fc.q, corr = fc.corr;
             // n mod q_f = b2 + T1[d1] + S0[slot] mod q_f, with -M mod q_f per wrap
-            uint32_t x = red2(bqv[j] + C.sTQ1[d1 * ES_FMAX + f] + (wrap1 ? corr : 0u), q);
-            x = red2(x + C.sQ0[f * r0 + slot] + (cw ? corr : 0u), q);
+            uint32_t x = red2(bqv[j] + sTQ1[d1 * ES_FMAX + f] + (wrap1 ? corr : 0u), q);
+            x = red2(x + sQ0[f * r0 + slot] + (cw ? corr : 0u), q);
             const uint32_t wv = __ldg(C.allowed_g + fc.off + (x >> 5));
             ok = ok && ((wv >> (x & 31u)) & 1u);
             if (COUNT && ok) red_add_shared(C.wcnt_saddr + 4u * f, 1u);
@@ -289,11 +313,11 @@ __device__ __forceinline__ void flush(EsQueue* Q, uint32_t lane, uint32_t step, 
     }
     if (ok) {
         uint32_t wm;
-        const U4 b = addmod(u4(Q->rec[own][0]), u4(C.sT1[d1]), C.M, wm);
-        const U4 s = addmod(b, u4(C.sS0[slot]), C.M, wm);
+        const U4 b = addmod(u4(Q->rec[own][0]), u4(sT1[d1]), C.M, wm);
+        const U4 s = addmod(b, u4(sS0[slot]), C.M, wm);
         const uint64_t e = C.e_base + (uint64_t)own * C.strip + step;
         const uint64_t oidx = C.list ? __ldg(C.list + e) : e * C.r1 + d1;
-        tail_one<COUNT>(C, fr, s, oidx * (uint64_t)r0 + C.sI0[slot]);
+        tail_one<COUNT>(C, sFC, fr, s, oidx * (uint64_t)r0 + sI0[slot]);
     }
     __syncwarp();
 }
@@ -301,7 +325,8 @@ __device__ __forceinline__ void flush(EsQueue* Q, uint32_t lane, uint32_t step, 
 // warp-uniform (has = ballot of (lo | hi) != 0, nonzero; qsize < 32 on entry): queue the word
 // pair (wd, wd + 1) of every lane that has candidates, then flush while 32 entries are waiting
 template <bool COUNT>
-__device__ __forceinline__ void push(EsQueue* Q, uint32_t lane, uint32_t step, uint32_t& qhead,
+__device__ __forceinline__ void push(EsQueue* Q, const unsigned char* smem, const EsInst& si, uint32_t lane,
+                                     uint32_t step, uint32_t& qhead,
                                      uint32_t& qsize, uint32_t has, uint32_t lo, uint32_t hi,
                                      uint32_t split, uint32_t d1, uint32_t wd, uint32_t wm1) {
     if (lo | hi) {
@@ -310,7 +335,7 @@ __device__ __forceinline__ void push(EsQueue* Q, uint32_t lane, uint32_t step, u
     }
     qsize += __popc(has);
     // each pass retires one candidate per lane, so this ends
-    while (qsize >= 32u) flush<COUNT>(Q, lane, step, qhead, qsize);
+    while (qsize >= 32u) flush<COUNT>(Q, smem, si, lane, step, qhead, qsize);
 }
 
 // Warp-uniform: scan one warp-unit w of `item`, whose plan is staged in smem / si.
@@ -326,16 +351,11 @@ __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, u
     const uint32_t r0 = si.r0, r1 = si.r1, r2 = si.r2;
     const uint32_t Wn = WT ? (uint32_t)WT : si.W;
     const uint32_t bsh = si.bsh, tail = si.tail_mask;
-    const uint32_t kl = si.sh >> 5, ko = si.sh & 31u;   // key = 32 bits of thr from bit sh
     const uint32_t* __restrict__ masks_g = si.masks;
-    const uint4* sT1 = reinterpret_cast<const uint4*>(smem + si.o_T1);
     const uint4* sTQ1 = reinterpret_cast<const uint4*>(smem + si.o_TQ1);
     const uint4* sD2 = reinterpret_cast<const uint4*>(smem + si.o_D2);
     const uint4* sDQ2 = reinterpret_cast<const uint4*>(smem + si.o_DQ2);
     const uint32_t* sDQ2w = reinterpret_cast<const uint32_t*>(sDQ2);
-    const uint4* sS0 = reinterpret_cast<const uint4*>(smem + si.o_S0);
-    const uint32_t* sK0 = reinterpret_cast<const uint32_t*>(smem + si.o_K0);
-    const uint32_t* sI0 = reinterpret_cast<const uint32_t*>(smem + si.o_I0);
     const uint32_t* sQ0 = reinterpret_cast<const uint32_t*>(smem + si.o_Q0);
     const uint4* sBK = reinterpret_cast<const uint4*>(smem + si.o_BK);   // {slot, 3 keys}
     const uint32_t* sK1 = reinterpret_cast<const uint32_t*>(smem + si.o_K1);
@@ -359,12 +379,6 @@ __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, u
         C.M_big = (si.M_hi != 0) || (si.M_lo > C.kp1);
         C.nf = nf;
         C.r0 = si.r0;
-        C.sT1 = reinterpret_cast<const uint4*>(smem + si.o_T1);
-        C.sS0 = reinterpret_cast<const uint4*>(smem + si.o_S0);
-        C.sI0 = reinterpret_cast<const uint32_t*>(smem + si.o_I0);
-        C.sTQ1 = reinterpret_cast<const uint32_t*>(smem + si.o_TQ1);
-        C.sQ0 = reinterpret_cast<const uint32_t*>(smem + si.o_Q0);
-        C.sFC = sFC;
         C.tc = tcv;
         C.allowed_g = si.allowed;
         C.surv = L.surv;
@@ -409,7 +423,6 @@ __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, u
         e_hi = e_lo + L.strip;
         if (e_hi > item.c_end) e_hi = item.c_end;
     }
-    U4 b2{0u, 0u, 0u, 0u};
     uint32_t d2 = 0;
     uint32_t BQ2[FA];
 #pragma unroll
@@ -423,6 +436,9 @@ __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, u
         if (__ballot_sync(0xffffffffu, live) == 0u) break;
         uint64_t c = prev_c;
         uint32_t lo1 = 0u, hi1 = 0u;
+        // b2 of the lane's last cycle lives in its record (0 before the first decode)
+        const U4 Mv = ldv_M(si);
+        U4 b2 = have ? ldv128(&Q->rec[lane][0]) : U4{0u, 0u, 0u, 0u};
         if (live) {
             if (list) {
                 const uint64_t o = __ldg(reinterpret_cast<const unsigned long long*>(list) + e);
@@ -439,7 +455,7 @@ __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, u
             // rings >= 2: one delta step while the ring-2 digit advances, else a decode
             if (have && c == prev_c + 1 && d2 + 1u < r2) {
                 uint32_t wm;
-                b2 = addmod(b2, u4(sD2[d2]), M, wm);
+                b2 = addmod(b2, u4(sD2[d2]), Mv, wm);
                 uint32_t dq[8];
                 row8<F>(sDQ2 + d2 * (ES_FMAX / 4), dq);
 #pragma unroll
@@ -456,7 +472,7 @@ __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, u
                 Q->rec[lane][1] = make_uint4(rv[0], rv[1], rv[2], rv[3]);
                 ++d2;
             } else if (!(have && c == prev_c)) {
-                b2 = decode_cycle(si, c, M, d2);
+                b2 = decode_cycle(si, c, Mv, d2);
 #pragma unroll
                 for (int f = 0; f < F; ++f) {
                     if ((uint32_t)f < Feff) BQ2[f] = red1(mod128(b2, sFC[f]) + tcv[f], qf[f]);
@@ -475,9 +491,7 @@ __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, u
         }
         // A = M - b2 and its 32-bit key, once per ring-1 cycle
         uint32_t brA;
-        const U4 A = sub128(M, b2, brA);
-        const uint32_t KA = __funnelshift_r(kl == 0 ? A.x : (kl == 1 ? A.y : A.z),
-                                            kl == 0 ? A.y : (kl == 1 ? A.z : A.w), ko);
+        const uint32_t KA = key32(sub128(Mv, b2, brA), ldv32(&si.sh));
 
         // ---- ring 1: warp-uniform sweep (broadcast loads) --------------------------------
         for (uint32_t d1 = 0; d1 < r1; ++d1) {
@@ -500,18 +514,21 @@ __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, u
             uint32_t split = bk.x + (s1 ? 1u : 0u) + (s2 ? 1u : 0u);
             const uint32_t ks = s2 ? bk.w : (s1 ? bk.z : bk.y);   // key of slot `split`
             // rare: a key tie with A, a key inside the +-1 band, or a crowded bucket -> exact
-            const bool rare = (k1 == KA) || (ks <= th);
+            // (only lanes with candidates here: their record holds b2)
+            const bool rare = act && ((k1 == KA) || (ks <= th));
             if (__any_sync(0xffffffffu, rare)) {
                 if (rare) {
                     uint32_t wx, brw;
-                    const U4 b = addmod(b2, u4(sT1[d1]), M, wx);
+                    const U4 Mr = ldv_M(si);
+                    const U4 b = addmod(ldv128(&Q->rec[lane][0]), ldv128(smem + ldv32(&si.o_T1) + 16u * d1), Mr, wx);
                     wm1 = wx;
-                    const U4 thr = sub128(M, b, brw);
-                    const uint32_t te = __funnelshift_r(kl == 0 ? thr.x : (kl == 1 ? thr.y : thr.z),
-                                                        kl == 0 ? thr.y : (kl == 1 ? thr.z : thr.w), ko);
+                    const U4 thr = sub128(Mr, b, brw);
+                    const uint32_t te = key32(thr, ldv32(&si.sh));
+                    const uint32_t* rK0 = reinterpret_cast<const uint32_t*>(smem + ldv32(&si.o_K0));
+                    const uint4* rS0 = reinterpret_cast<const uint4*>(smem + ldv32(&si.o_S0));
                     split = sBK[te >> bsh].x;
-                    while (sK0[split] < te) ++split;
-                    while (sK0[split] == te && lt128(u4(sS0[split]), thr)) ++split;   // S0[r0] = M stops it
+                    while (rK0[split] < te) ++split;
+                    while (rK0[split] == te && lt128(u4(rS0[split]), thr)) ++split;   // S0[r0] = M stops it
                 }
             }
 
@@ -562,11 +579,11 @@ __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, u
                 const bool odd = (wd & 1u) != 0u;
                 const uint32_t plo = odd ? lo : bits, phi = odd ? bits : 0u;
                 const uint32_t has = __ballot_sync(0xffffffffu, (plo | phi) != 0u);
-                if (has) push<COUNT>(Q, lane, step, qhead, qsize, has, plo, phi, split, d1, wd & ~1u, wm1);
+                if (has) push<COUNT>(Q, smem, si, lane, step, qhead, qsize, has, plo, phi, split, d1, wd & ~1u, wm1);
             }
         }
         // the records change with the next strip step: drain the queue
-        while (qsize) flush<COUNT>(Q, lane, step, qhead, qsize);
+        while (qsize) flush<COUNT>(Q, smem, si, lane, step, qhead, qsize);
     }
     // ---- per-stage counts of this warp-unit into the item's totals ----------------------
     if (COUNT) {
