@@ -40,7 +40,12 @@ LOG2_POS = 34
 # DRAM bytes per scan launch of this workload (dram__bytes_read.sum + dram__bytes_write.sum, one
 # ncu capture on GB300 of the 2^30-position case): the scan reads only its plan tables, once, so
 # the figure does not grow with the range (algorithmic HBM bytes per candidate: zero).
-TABLE_TRAFFIC_BYTES = 265216 + 768
+TABLE_TRAFFIC_BYTES = 283648 + 256
+# Warp instructions the scan kernel issues per candidate on this workload (smsp__inst_executed.sum
+# / positions, the same ncu capture): with the measured SM clock it gives the kernel's issue rate
+# against the issue peak (4 schedulers x 1 warp instruction per clock per SM), the bound that an
+# integer kernel with no DRAM or tensor work actually meets.
+WARP_INST_PER_CANDIDATE = 184941830 / 2 ** 30
 METRIC = "Gcand/s on 1 GB300 (% int peak)"
 
 
@@ -289,8 +294,16 @@ def main():
     evals = total + sum(counts[:-1]) if counts else total
     fbar = evals / total
     W = 10 + 8 * fbar
-    achieved = value * 1e9 * W / 1e12
+    achieved = value / world * 1e9 * W / 1e12   # per GPU, against one GPU's peak
     peak = peak_ops / 1e12
+    sm_hz = (clocks.get("sm_mhz") or clocks.get("sm_max_mhz") or 0) * 1e6
+    issue_peak = dev["sm_count"] * 4 * sm_hz
+    issue_ach = value / world * 1e9 * WARP_INST_PER_CANDIDATE
+    issue = {"achieved": issue_ach / 1e12, "peak": issue_peak / 1e12 if issue_peak else None,
+             "unit": "T warp-inst/s", "frac": issue_ach / issue_peak if issue_peak else None,
+             "warp_inst_per_candidate": WARP_INST_PER_CANDIDATE,
+             "source": "instructions per candidate from an ncu capture of this kernel on the "
+                       "2^30-position case; issue peak = SMs x 4 schedulers x SM clock sampled here"}
     line = {
         "metric": METRIC, "value": value, "unit": "Gcand/s", "n_gpus": world, "steps": args.steps,
         "warmup": max(3, args.warmup), "ms_per_step": ms_step, "higher_is_better": True,
@@ -306,8 +319,11 @@ def main():
         "gpu_launches": args.steps,
         "roofline": {"bound": "int32", "achieved": achieved, "peak": peak, "unit": "Tops/s",
                      "frac": achieved / peak, "traffic": TABLE_TRAFFIC_BYTES,
-                     "model": f"W=10+8*fbar int32 ops/candidate, fbar={fbar:.4f} (this run's stage counts)",
-                     "peak_source": "measured: es_int_peak IADD3/LOP3 microbenchmark, this run"},
+                     "model": f"W=10+8*fbar int32 ops/candidate, fbar={fbar:.4f} (this run's stage counts); "
+                              "the word-mask cascade tests 32 candidates per table load, so it exceeds "
+                              "this scalar-cascade model (frac > 1)",
+                     "peak_source": "measured: es_int_peak IADD3/LOP3 microbenchmark, this run",
+                     "issue": issue},
         "clocks": clocks,
         "survivors_per_step": n_surv,
         "stage_counts_first8": counts[:8],
