@@ -46,6 +46,10 @@ TABLE_TRAFFIC_BYTES = 283648 + 256
 # against the issue peak (4 schedulers x 1 warp instruction per clock per SM), the bound that an
 # integer kernel with no DRAM or tensor work actually meets.
 WARP_INST_PER_CANDIDATE = 184941830 / 2 ** 30
+# Integer thread-instructions the scan kernel executes per candidate on this workload
+# (sm__sass_thread_inst_executed_op_integer_pred_on.sum / positions, an ncu capture of the same
+# 2^30-position case): the achieved integer-op rate against the measured int32 peak.
+INT_THREAD_OPS_PER_CANDIDATE = 3136909549 / 2 ** 30
 METRIC = "Gcand/s on 1 GB300 (% int peak)"
 
 
@@ -304,6 +308,12 @@ def main():
              "warp_inst_per_candidate": WARP_INST_PER_CANDIDATE,
              "source": "instructions per candidate from an ncu capture of this kernel on the "
                        "2^30-position case; issue peak = SMs x 4 schedulers x SM clock sampled here"}
+    int_ach = value / world * 1e9 * INT_THREAD_OPS_PER_CANDIDATE
+    int_pipe = {"achieved": int_ach / 1e12, "peak": peak, "unit": "T int-ops/s", "frac": int_ach / peak_ops,
+                "int_thread_ops_per_candidate": INT_THREAD_OPS_PER_CANDIDATE,
+                "source": "executed integer thread-instructions per candidate (ncu "
+                          "sm__sass_thread_inst_executed_op_integer_pred_on) x Gcand/s, against the "
+                          "es_int_peak measurement of this run"}
     line = {
         "metric": METRIC, "value": value, "unit": "Gcand/s", "n_gpus": world, "steps": args.steps,
         "warmup": max(3, args.warmup), "ms_per_step": ms_step, "higher_is_better": True,
@@ -323,7 +333,7 @@ def main():
                               "the word-mask cascade tests 32 candidates per table load, so it exceeds "
                               "this scalar-cascade model (frac > 1)",
                      "peak_source": "measured: es_int_peak IADD3/LOP3 microbenchmark, this run",
-                     "issue": issue},
+                     "issue": issue, "int_pipe": int_pipe},
         "clocks": clocks,
         "survivors_per_step": n_surv,
         "stage_counts_first8": counts[:8],
