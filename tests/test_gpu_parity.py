@@ -144,6 +144,21 @@ def test_batch64_prefixes(native):
         b.close()
 
 
+def test_batch64_config_items_match_c_oracle(native):
+    """Config 3 as the measurement runs it (one persistent launch over the 64 seeded instances,
+    each with its full range): every instance of at most 2^24 positions, survivors and per-stage
+    counts, against the C oracle of the reference path."""
+    import es_configs
+    import es_gb300
+    import es_oracle as O
+    res = es_configs.batch64(autotune=False, reps=1)
+    assert res["instances"] == 64 and len(res["small_items"]) >= 16
+    for it in res["small_items"]:
+        ws, wc, _ = O.scan_c(es_gb300.Plan(it["k"]), 0, o_range=tuple(it["o_range"]))
+        assert it["survivors"] == ws, it["item"]
+        assert it["counts"] == wc, it["item"]
+
+
 def test_search_matches_bfile(native, bfile):
     """Drop-in search() reproduces g(k) for k = 1..140 (harness/gate.py semantics)."""
     import es_gb300
