@@ -532,6 +532,26 @@ __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, u
                 }
             }
 
+            if (LAYOUT == ES_LAYOUT_WORDMASK && WT == 2) {
+                // two inner words: both words of a phase are adjacent in P_f, so one 8-byte load
+                // per filter and phase serves them, and the pair is queued as one entry
+                uint32_t b0 = act ? 0xffffffffu : 0u, b1 = act ? tail : 0u;
+                const uint32_t cm0 = __funnelshift_lc(0u, 0xffffffffu, split);
+                const uint32_t cm1 = __funnelshift_lc(0u, 0xffffffffu, max(split, 32u) - 32u) & tail;
+#pragma unroll
+                for (int f = 0; f < F; ++f) {
+                    const uint32_t x0 = red2(BQ2[f] + tq[f] + (corr[f] & wm1), qf[f]);
+                    const uint32_t x1 = red1(x0 + corr[f], qf[f]);
+                    const uint2 m0 = __ldg(reinterpret_cast<const uint2*>(tab[f]) + x0);
+                    const uint2 m1 = __ldg(reinterpret_cast<const uint2*>(tab[f]) + x1);
+                    b0 &= (m0.x & ~cm0) | (m1.x & cm0);
+                    b1 &= (m0.y & ~cm1) | (m1.y & cm1);
+                    if (COUNT) cnt[f] += __popc(b0) + __popc(b1);
+                }
+                const uint32_t has = __ballot_sync(0xffffffffu, (b0 | b1) != 0u);
+                if (has) push<COUNT>(Q, smem, si, lane, step, qhead, qsize, has, b0, b1, split, d1, 0u, wm1);
+                continue;
+            }
             uint32_t lo = 0u;   // bits of an even word, queued with the odd word after it
             for (uint32_t wd = 0; wd < Wn; ++wd) {
                 const uint32_t valid = (wd + 1u == Wn) ? tail : 0xffffffffu;
