@@ -1,6 +1,7 @@
 #!/usr/bin/env python3
-"""Build libes_gb300.so (sm_103a) in-tree with nvcc: the scan kernels, the host C ABI and the
-learned-planner MLP kernels, compiled in parallel, linked against the CUDA runtime.
+"""Build libes_gb300.so (sm_103a) in-tree with nvcc: the scan kernels (one translation unit per
+table layout), the host C ABI and the learned-planner MLP kernels, compiled in parallel, linked
+against the CUDA runtime.
 
     python erdos-selfridge_gb300/build.py [--force]
 
@@ -20,7 +21,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "libes_gb300.so")
 OBJDIR = os.path.join(HERE, "_build")
-SOURCES = ["es_scan.cu", "es_abi.cu", "es_mlp.cu"]
+SOURCES = ["es_scan_wm.cu", "es_scan_pair.cu", "es_scan_sc.cu", "es_scan.cu", "es_abi.cu", "es_mlp.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -77,8 +77,8 @@ int device_facts() {
 size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 int check_tune(const es_tune& t) {
-    if (t.layout != ES_LAYOUT_WORDMASK && t.layout != ES_LAYOUT_SCALAR)
-        return fail(ES_ERR_ARG, "tune.layout must be 0 (word-mask) or 1 (scalar)");
+    if (t.layout != ES_LAYOUT_WORDMASK && t.layout != ES_LAYOUT_SCALAR && t.layout != ES_LAYOUT_PAIR)
+        return fail(ES_ERR_ARG, "tune.layout must be 0 (word-mask), 1 (scalar) or 2 (pair)");
     if (t.mask_filters < 1 || t.mask_filters > ES_MAX_MASK_FILTERS)
         return fail(ES_ERR_ARG, "tune.mask_filters must be in 1..8");
     if (t.threads < 64 || t.threads > 1024 || t.threads % 32)
@@ -429,6 +429,25 @@ int es_ctx_create(const es_plan_desc* d, const es_tune* tune_in, es_ctx** out) {
         }
     }
     c->fast_words_mask.assign(mask_off.begin(), mask_off.begin() + FB + 1);
+    // pair tables (inner rings of at most two words): phase row phi holds P_f[phi] and then the
+    // row a wrap past M selects, P_f[(phi + corr_f) mod q_f], so one load serves both sides of
+    // the carry split; filter f starts at word 2 * mask_off[f]
+    std::vector<uint32_t> pairs;
+    if (W <= 2) {
+        pairs.assign(2ull * masks.size(), 0u);
+        for (uint32_t f = 0; f < FB; ++f) {
+            const uint32_t q = c->q[f], corr = fc[f].corr;
+            const uint32_t* P = masks.data() + mask_off[f];
+            uint32_t* D = pairs.data() + 2ull * mask_off[f];
+            for (uint32_t ph = 0; ph < q; ++ph) {
+                const uint32_t ph1 = (uint32_t)(((uint64_t)ph + corr) % q);
+                for (uint32_t wd = 0; wd < W; ++wd) {
+                    D[(uint64_t)ph * 2 * W + wd] = P[(uint64_t)ph * W + wd];
+                    D[(uint64_t)ph * 2 * W + W + wd] = P[(uint64_t)ph1 * W + wd];
+                }
+            }
+        }
+    }
 
     // ---- arena ----------------------------------------------------------------------------
     size_t aoff = 0;
@@ -436,6 +455,7 @@ int es_ctx_create(const es_plan_desc* d, const es_tune* tune_in, es_ctx** out) {
     const size_t a_inst = atake(sizeof(EsInst));
     const size_t a_small = atake(small_bytes);
     const size_t a_masks = atake(4ull * masks.size());
+    const size_t a_pairs = atake(4ull * std::max<size_t>(pairs.size(), 4));
     const size_t a_bits = atake(4ull * std::max<uint32_t>(bit_off[nf], 4));
     const size_t a_terms = atake(16ull * terms.size());
     const size_t a_roff = atake(4ull * nr);
@@ -444,6 +464,7 @@ int es_ctx_create(const es_plan_desc* d, const es_tune* tune_in, es_ctx** out) {
     std::vector<unsigned char> img(aoff, 0);
     memcpy(&img[a_small], small.data(), small_bytes);
     memcpy(&img[a_masks], masks.data(), 4ull * masks.size());
+    if (!pairs.empty()) memcpy(&img[a_pairs], pairs.data(), 4ull * pairs.size());
     if (bit_off[nf]) memcpy(&img[a_bits], d->allowed, 4ull * bit_off[nf]);
     for (size_t i = 0; i < terms.size(); ++i) {
         uint64_t lo = (uint64_t)terms[i], hi = (uint64_t)(terms[i] >> 64);
@@ -472,6 +493,7 @@ int es_ctx_create(const es_plan_desc* d, const es_tune* tune_in, es_ctx** out) {
     for (uint32_t f = 0; f <= ES_FMAX; ++f) I.mask_off[f] = mask_off[f];
     I.small = c->d_arena + a_small;
     I.masks = reinterpret_cast<const uint32_t*>(c->d_arena + a_masks);
+    I.pairs = reinterpret_cast<const uint32_t*>(c->d_arena + a_pairs);
     I.allowed = reinterpret_cast<const uint32_t*>(c->d_arena + a_bits);
     I.ring_terms = reinterpret_cast<const uint64_t*>(c->d_arena + a_terms);
     I.ring_off = reinterpret_cast<const uint32_t*>(c->d_arena + a_roff);

@@ -60,6 +60,7 @@ struct EsInst {
     uint32_t pad0;
     const unsigned char* small;      // device copy of the small block
     const uint32_t* masks;           // word-mask tables
+    const uint32_t* pairs;           // pair tables (W <= 2): row phi = P_f[phi], P_f[(phi + corr_f) mod q_f]
     const uint32_t* allowed;         // bit tables of all filters
     const uint64_t* ring_terms;      // [sum radix][2] lo,hi
     const uint32_t* ring_off;        // [n_rings]
@@ -108,6 +109,12 @@ struct EsLaunch {
     EsItem item0;
     uint32_t tconst0[ES_MAX_FILTERS];
 };
+
+// Scan kernel instances by layout (es_scan_wm.cu, es_scan_pair.cu, es_scan_sc.cu).
+typedef void (*ScanFn)(const EsLaunch);
+ScanFn es_pick_wordmask(int count, uint32_t words, uint32_t mask_filters);
+ScanFn es_pick_pair(int count, uint32_t words, uint32_t mask_filters);
+ScanFn es_pick_scalar(int count, uint32_t mask_filters);
 
 // Host-side launchers implemented in es_scan.cu (return a cudaError_t value).
 int es_scan_prepare(int smem_optin_bytes);

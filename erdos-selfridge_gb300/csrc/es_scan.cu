@@ -1,36 +1,6 @@
-// Device kernels of the GB300 Erdős–Selfridge CRT-wheel sieve (sm_103a).
-//
-// What one launch computes (semantics of the reference kernel, sieve/gpu_sieve_v9.py:240-330,
-// sieve/gpu_sieve_v11.py:250-354, sieve/es_word_masks.py:39-92): for every work item (a plan,
-// a block t, an outer-index range) and every position idx = oidx*r0 + d0 in the range,
-//   n = t*M + ((sum_j term_j[d_j]) mod M)        (mixed radix, ring 0 fastest)
-// passes iff (n mod q_f) is admissible for every residual filter f, in cascade order.
-// Survivors are emitted with their ORIGINAL inner digit d0; per-stage pass counts are
-// accumulated on request.  All arithmetic is exact integer arithmetic.
-//
-// How it is organised (GB300-first, not the reference's per-plan NVRTC source):
-//  * One persistent kernel per launch; warps claim work units from a global atomic counter --
-//    no spin waits anywhere.  Items are ordered by (group, block), and a group's later blocks
-//    are skipped once a good survivor is known (block-ordered search).
-//  * Two-level strip mining.  A lane owns `strip` consecutive ring-1 cycles (cycle index =
-//    oidx / r1).  Rings >= 2 give b2 = sum term_j mod M, decoded once per strip and then
-//    stepped with a 128-bit delta table when the ring-2 digit advances.  Ring 1 is swept in a
-//    warp-uniform loop (b = b2 + T1[d1], broadcast loads) and ring 0, the inner ring, is
-//    handled 32 candidates at a time as bit masks.
-//  * 128-bit values are four 32-bit limbs with PTX carry chains; filter residues are carried
-//    incrementally in 32-bit arithmetic: BQ_f = n mod q_f for the ring-0 base, updated from
-//    precomputed term residues and the wrap correction corr_f = -M mod q_f (the reference's v7
-//    identity, sieve/gpu_sieve_v9.py:9-18), reduced with unsigned min instead of branches.
-//  * Inner ring: its terms are sorted once on the host, so the wrap (s >= M) is a suffix of the
-//    sorted slots; its start (the carry split) comes from 32-bit keys through a 512-bucket
-//    table.  Word-mask layout: a filter costs two table loads per 32 candidates,
-//    P_f[phase][w]; scalar layout: one residue + bit test per live candidate.  A warp leaves
-//    the cascade early when a ballot shows no live candidate.
-//  * Inner words that still hold candidates after the inner-ring stage are queued per warp as
-//    one 16-byte entry per lane; a flush takes 32 entries, one candidate per lane (full warps,
-//    not single lanes), runs the next filters from 32-bit term residues, and gives only the
-//    few candidates left the exact tail: n mod M rebuilt in 128 bits, then limb weights and a
-//    Barrett reduction per filter.
+// Dispatch of the scan kernel instances, the block-ordered min-reduction and the integer-pipe
+// peak probe of the GB300 Erdős–Selfridge CRT-wheel sieve (sm_103a).  The scan kernel itself is
+// es_scan_kernel.cuh, instantiated per layout in es_scan_wm.cu, es_scan_pair.cu, es_scan_sc.cu.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -38,724 +8,6 @@
 #include "es_internal.h"
 
 namespace {
-
-// 128-bit value as little-endian 32-bit limbs.
-struct U4 {
-    uint32_t x, y, z, w;
-};
-
-__device__ __forceinline__ U4 u4(const uint4 v) { return U4{v.x, v.y, v.z, v.w}; }
-
-__device__ __forceinline__ U4 add128(const U4 a, const U4 b) {
-    U4 r;
-    asm("add.cc.u32 %0, %4, %8;\n\t"
-        "addc.cc.u32 %1, %5, %9;\n\t"
-        "addc.cc.u32 %2, %6, %10;\n\t"
-        "addc.u32 %3, %7, %11;"
-        : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w)
-        : "r"(a.x), "r"(a.y), "r"(a.z), "r"(a.w), "r"(b.x), "r"(b.y), "r"(b.z), "r"(b.w));
-    return r;
-}
-
-// r = a - b; borrow = 0xffffffff when a < b, else 0.
-__device__ __forceinline__ U4 sub128(const U4 a, const U4 b, uint32_t& borrow) {
-    U4 r;
-    asm("sub.cc.u32 %0, %5, %9;\n\t"
-        "subc.cc.u32 %1, %6, %10;\n\t"
-        "subc.cc.u32 %2, %7, %11;\n\t"
-        "subc.cc.u32 %3, %8, %12;\n\t"
-        "subc.u32 %4, 0, 0;"
-        : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w), "=r"(borrow)
-        : "r"(a.x), "r"(a.y), "r"(a.z), "r"(a.w), "r"(b.x), "r"(b.y), "r"(b.z), "r"(b.w));
-    return r;
-}
-
-__device__ __forceinline__ U4 sel128(uint32_t mask, const U4 a, const U4 b) {  // mask ? a : b
-    return U4{(a.x & mask) | (b.x & ~mask), (a.y & mask) | (b.y & ~mask), (a.z & mask) | (b.z & ~mask),
-              (a.w & mask) | (b.w & ~mask)};
-}
-
-// (a + b) mod M for a, b < M < 2^126; wmask = 0xffffffff when M was subtracted.
-__device__ __forceinline__ U4 addmod(const U4 a, const U4 b, const U4 M, uint32_t& wmask) {
-    const U4 s = add128(a, b);
-    uint32_t br;
-    const U4 d = sub128(s, M, br);
-    wmask = ~br;
-    return sel128(br, s, d);
-}
-
-__device__ __forceinline__ bool lt128(const U4 a, const U4 b) {
-    uint32_t br;
-    sub128(a, b, br);
-    return br != 0u;
-}
-
-__device__ __forceinline__ uint64_t lo64(const U4 a) { return ((uint64_t)a.y << 32) | a.x; }
-__device__ __forceinline__ uint64_t hi64(const U4 a) { return ((uint64_t)a.w << 32) | a.z; }
-
-// x mod q for a 128-bit x, q < 2^20: limb weights (2^32i mod q) then one Barrett step.
-__device__ __forceinline__ uint32_t mod128(const U4 x, const EsFilterC& f) {
-    const uint64_t y = (uint64_t)x.x + (uint64_t)x.y * f.w1 + (uint64_t)x.z * f.w2 + (uint64_t)x.w * f.w3;
-    const uint64_t qt = __umul64hi(y, f.rcp);
-    uint64_t r = y - qt * f.q;
-    if (r >= f.q) r -= f.q;
-    return (uint32_t)r;
-}
-
-// v mod q for v < 2q (unsigned min: v - q wraps to a huge value when v < q)
-__device__ __forceinline__ uint32_t red1(uint32_t v, uint32_t q) { return min(v, v - q); }
-// v mod q for v < 3q
-__device__ __forceinline__ uint32_t red2(uint32_t v, uint32_t q) { return red1(red1(v, q), q); }
-
-// Volatile shared loads: values the ring-1 sweep needs only on its rare paths are re-read where
-// they are used instead of being held in registers across the sweep.
-__device__ __forceinline__ uint32_t ldv32(const void* p) {
-    uint32_t v;
-    asm volatile("ld.volatile.shared.u32 %0, [%1];" : "=r"(v) : "r"((uint32_t)__cvta_generic_to_shared(p)));
-    return v;
-}
-__device__ __forceinline__ U4 ldv128(const void* p) {
-    U4 v;
-    asm volatile("ld.volatile.shared.v4.u32 {%0, %1, %2, %3}, [%4];"
-                 : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
-                 : "r"((uint32_t)__cvta_generic_to_shared(p)));
-    return v;
-}
-__device__ __forceinline__ U4 ldv_M(const EsInst& si) {   // M_lo, M_hi are adjacent
-    return ldv128(&si.M_lo);
-}
-// 32 bits of x from bit sh (sh < 96): the carry-split key
-__device__ __forceinline__ uint32_t key32(const U4 x, uint32_t sh) {
-    const uint32_t kl = sh >> 5, ko = sh & 31u;
-    return __funnelshift_r(kl == 0 ? x.x : (kl == 1 ? x.y : x.z), kl == 0 ? x.y : (kl == 1 ? x.z : x.w), ko);
-}
-
-// b2 = sum_{j>=2} term_j[d_j] mod M for ring-1 cycle c; also returns the ring-2 digit.
-__device__ __noinline__ U4 decode_cycle(const EsInst& I, uint64_t c, const U4 M, uint32_t& d2) {
-    uint64_t rem = c;
-    U4 acc{0u, 0u, 0u, 0u};
-    d2 = 0;
-    for (uint32_t j = 2; j < I.n_rings; ++j) {
-        const uint32_t r = __ldg(I.radix + j);
-        uint64_t d;
-        if ((rem >> 32) == 0) {
-            const uint32_t r32 = (uint32_t)rem;
-            d = r32 % r;
-            rem = r32 / r;
-        } else {
-            d = rem % r;
-            rem = rem / r;
-        }
-        if (j == 2) d2 = (uint32_t)d;
-        const uint4 tv = __ldg(reinterpret_cast<const uint4*>(I.ring_terms) + (__ldg(I.ring_off + j) + d));
-        uint32_t wm;
-        acc = addmod(acc, u4(tv), M, wm);
-    }
-    return acc;
-}
-
-__device__ __forceinline__ void copy_words(uint32_t* dst, const uint32_t* __restrict__ src,
-                                           uint32_t nwords) {
-    // 16-byte vector copies (both ends 16-byte aligned by construction), then the tail
-    const uint32_t n4 = nwords >> 2;
-    const uint4* s4 = reinterpret_cast<const uint4*>(src);
-    uint4* d4 = reinterpret_cast<uint4*>(dst);
-    for (uint32_t i = threadIdx.x; i < n4; i += blockDim.x) d4[i] = __ldg(s4 + i);
-    for (uint32_t i = (n4 << 2) + threadIdx.x; i < nwords; i += blockDim.x) dst[i] = __ldg(src + i);
-}
-
-// Everything the flush, the cascade tail and the emit need for one warp-unit.  It lives in the
-// warp's slot in shared memory, written once per warp-unit and read only on the flush path, so
-// none of it occupies registers across the ring-1 sweep.
-struct TailCtx {
-    U4 M;
-    uint64_t M_lo;
-    uint64_t t_blk;
-    uint64_t e_base;                   // strip entry of lane 0 (ring-1 cycle or list position)
-    const unsigned long long* list;    // outer-index list of the item, or null (a range)
-    const uint32_t* tc;
-    const uint32_t* allowed_g;
-    es_survivor* surv;
-    unsigned long long* surv_n;
-    unsigned long long* group_found;
-    uint64_t surv_cap;
-    uint32_t kp1, Feff, FR, nf, wcnt_saddr, item_id, group, r0, r1, strip;
-    bool M_big;
-};
-
-// Per-warp queue of inner-word pairs that still hold candidates after the inner-ring stage.  An
-// entry is one lane's words w, w+1 of one outer index: {candidate bits of word w, of word w+1,
-// d1 | carry split << 16, lane | ring-1 wrap << 5 | w << 6}.
-// The lane's ring-1 cycle is described once per strip step by its record (b2 and the residues
-// of b2 for the residue-stage filters), so a push is one 16-byte store per lane; the queue is
-// drained before the records change.  The flush runs 32 entries at a time (whole warps): first
-// the next ES_NRES filters from 32-bit residues (the tables of the inner-ring stage carry them),
-// then, for the few candidates left, n mod M and the exact tail.
-#define ES_QCAP 64
-#define ES_NRES 4
-struct EsQueue {
-    uint4 ent[ES_QCAP];
-    uint4 rec[32][2];                  // per lane: b2 (limbs); residues of b2 + block term
-    TailCtx ctx;                       // the warp's current item (see TailCtx)
-};
-static_assert(sizeof(EsQueue) <= ES_QUEUE_BYTES, "per-warp slot overflows its shared-memory share");
-
-__device__ __forceinline__ void red_add_shared(uint32_t saddr, uint32_t v) {
-    // Not visible to the compiler as a store: the counters are read only after a __syncwarp.
-    asm volatile("red.shared.add.u32 [%0], %1;" ::"r"(saddr), "r"(v));
-}
-
-#ifndef ES_LB_THREADS
-#define ES_LB_THREADS 512   // largest CTA the scan kernel is compiled for
-#endif
-#ifndef ES_LB_MINB
-#define ES_LB_MINB 1
-#endif
-
-// First F entries of an 8-entry residue row (two 16-byte loads at most).
-template <int F>
-__device__ __forceinline__ void row8(const uint4* row, uint32_t (&v)[8]) {
-    if (F > 0) {
-        const uint4 a = row[0];
-        v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
-    }
-    if (F > 4) {
-        const uint4 b = row[1];
-        v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
-    }
-}
-
-// exact tail of the cascade for one candidate (filters f0..nf-1), then the emit
-template <bool COUNT>
-__device__ __forceinline__ void tail_one(const TailCtx& C, const EsFilterC* sFC, uint32_t f0, const U4 s,
-                                         uint64_t idx) {
-    for (uint32_t f = f0; f < C.nf; ++f) {
-        const EsFilterC fc = sFC[f];
-        uint32_t r = mod128(s, fc) + C.tc[f];
-        if (r >= fc.q) r -= fc.q;
-        const uint32_t wv = __ldg(C.allowed_g + fc.off + (r >> 5));
-        if (!((wv >> (r & 31u)) & 1u)) return;
-        if (COUNT) red_add_shared(C.wcnt_saddr + 4u * f, 1u);
-    }
-    bool good;
-    if (C.M_big) {
-        good = (C.t_blk > 0) || s.w || s.z || s.y || (s.x > C.kp1);
-    } else {
-        const uint64_t n = C.t_blk * C.M_lo + s.x;   // M <= k+1 <= 1025: n fits easily
-        good = n > C.kp1;
-    }
-    const unsigned long long slot = atomicAdd(C.surv_n, 1ull);
-    if (slot < C.surv_cap) {
-        es_survivor* rec = C.surv + slot;
-        rec->idx = idx;
-        rec->s_lo = lo64(s);
-        rec->s_hi = hi64(s);
-        rec->t = C.t_blk;
-        rec->item = C.item_id;
-        rec->good = good ? 1u : 0u;
-    }
-    if (good && C.group_found) atomicMin(C.group_found + C.group, (unsigned long long)C.t_blk);
-}
-
-// warp-uniform: one pass over up to 32 queued entries.  Each lane takes the lowest candidate of
-// its entry (the rest of the entry goes back on the queue), so the residue stage runs converged
-// and the warp leaves it as soon as no lane has a live candidate; the few candidates left take
-// n mod M and the exact tail.
-template <bool COUNT>
-__device__ __forceinline__ void flush(EsQueue* Q, const unsigned char* smem, const EsInst& si, uint32_t lane,
-                                      uint32_t step, uint32_t& qhead, uint32_t& qsize) {
-    __syncwarp();
-    const TailCtx& C = Q->ctx;
-    const uint4* sT1 = reinterpret_cast<const uint4*>(smem + si.o_T1);
-    const uint4* sS0 = reinterpret_cast<const uint4*>(smem + si.o_S0);
-    const uint32_t* sI0 = reinterpret_cast<const uint32_t*>(smem + si.o_I0);
-    const uint32_t* sTQ1 = reinterpret_cast<const uint32_t*>(smem + si.o_TQ1);
-    const uint32_t* sQ0 = reinterpret_cast<const uint32_t*>(smem + si.o_Q0);
-    const EsFilterC* sFC = reinterpret_cast<const EsFilterC*>(smem + si.o_FC);
-    const uint32_t n = qsize < 32u ? qsize : 32u;
-    const uint4 en = Q->ent[(qhead + lane) & (ES_QCAP - 1)];
-    const uint64_t bits = lane < n ? ((uint64_t)en.y << 32) | en.x : 0ull;
-    const uint64_t rest = bits & (bits - 1ull);
-    const uint32_t back = __ballot_sync(0xffffffffu, rest != 0u);
-    __syncwarp();   // every lane holds its entry before any slot is reused
-    qhead = (qhead + n) & (ES_QCAP - 1);
-    qsize -= n;
-    if (rest) {
-        // lands on a free or just-consumed slot: qsize - n + popc(back) <= old qsize < ES_QCAP
-        const uint32_t pos = (qhead + qsize + __popc(back & ((1u << lane) - 1u))) & (ES_QCAP - 1);
-        Q->ent[pos] = make_uint4((uint32_t)rest, (uint32_t)(rest >> 32), en.z, en.w);
-    }
-    qsize += __popc(back);
-    const bool has = bits != 0ull;
-    const uint32_t i = has ? __ffsll((long long)bits) - 1u : 0u;
-    const uint32_t d1 = has ? (en.z & 0xffffu) : 0u;
-    const uint32_t slot = has ? ((en.w >> 6) << 5) + i : 0u;
-    const uint32_t own = has ? (en.w & 31u) : 0u;
-    const bool wrap1 = has && ((en.w >> 5) & 1u);
-    const bool cw = has && slot >= (en.z >> 16);   // sorted slots from the split on wrap past M
-    const uint4 bq = Q->rec[own][1];
-    const uint32_t bqv[ES_NRES] = {bq.x, bq.y, bq.z, bq.w};
-    const uint32_t f0 = C.Feff, fr = C.FR, r0 = C.r0;
-    bool ok = has;
-#pragma unroll
-    for (uint32_t j = 0; j < ES_NRES; ++j) {
-        const uint32_t f = f0 + j;
-        if (f < fr && __any_sync(0xffffffffu, ok)) {
-            const EsFilterC& fc = sFC[f];
-            const uint32_t q = fc.q, corr = fc.corr;
-            // n mod q_f = b2 + T1[d1] + S0[slot] mod q_f, with -M mod q_f per wrap
-            uint32_t x = red2(bqv[j] + sTQ1[d1 * ES_FMAX + f] + (wrap1 ? corr : 0u), q);
-            x = red2(x + sQ0[f * r0 + slot] + (cw ? corr : 0u), q);
-            const uint32_t wv = __ldg(C.allowed_g + fc.off + (x >> 5));
-            ok = ok && ((wv >> (x & 31u)) & 1u);
-            if (COUNT && ok) red_add_shared(C.wcnt_saddr + 4u * f, 1u);
-        }
-    }
-    if (ok) {
-        uint32_t wm;
-        const U4 b = addmod(u4(Q->rec[own][0]), u4(sT1[d1]), C.M, wm);
-        const U4 s = addmod(b, u4(sS0[slot]), C.M, wm);
-        const uint64_t e = C.e_base + (uint64_t)own * C.strip + step;
-        const uint64_t oidx = C.list ? __ldg(C.list + e) : e * C.r1 + d1;
-        tail_one<COUNT>(C, sFC, fr, s, oidx * (uint64_t)r0 + sI0[slot]);
-    }
-    __syncwarp();
-}
-
-// warp-uniform (has = ballot of (lo | hi) != 0, nonzero; qsize < 32 on entry): queue the word
-// pair (wd, wd + 1) of every lane that has candidates, then flush while 32 entries are waiting
-template <bool COUNT>
-__device__ __forceinline__ void push(EsQueue* Q, const unsigned char* smem, const EsInst& si, uint32_t lane,
-                                     uint32_t step, uint32_t& qhead,
-                                     uint32_t& qsize, uint32_t has, uint32_t lo, uint32_t hi,
-                                     uint32_t split, uint32_t d1, uint32_t wd, uint32_t wm1) {
-    if (lo | hi) {
-        const uint32_t pos = (qhead + qsize + __popc(has & ((1u << lane) - 1u))) & (ES_QCAP - 1);
-        Q->ent[pos] = make_uint4(lo, hi, d1 | (split << 16), lane | (wm1 & 32u) | (wd << 6));
-    }
-    qsize += __popc(has);
-    // each pass retires one candidate per lane, so this ends
-    while (qsize >= 32u) flush<COUNT>(Q, smem, si, lane, step, qhead, qsize);
-}
-
-// Warp-uniform: scan one warp-unit w of `item`, whose plan is staged in smem / si.
-template <int F, int LAYOUT, bool COUNT, int WT>
-__device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, unsigned char* smem,
-                                          EsQueue* Q, uint32_t* wcnt,
-                                          uint32_t wcnt_saddr, uint32_t lane, unsigned long long w,
-                                          const EsItem& item, uint32_t item_id) {
-    const U4 M{(uint32_t)si.M_lo, (uint32_t)(si.M_lo >> 32), (uint32_t)si.M_hi, (uint32_t)(si.M_hi >> 32)};
-    const EsFilterC* sFC = reinterpret_cast<const EsFilterC*>(smem + si.o_FC);
-    const uint32_t* tcv = L.items ? item.tconst : L.tconst0;
-    const uint32_t nf = si.n_filters;
-    const uint32_t r0 = si.r0, r1 = si.r1, r2 = si.r2;
-    const uint32_t Wn = WT ? (uint32_t)WT : si.W;
-    const uint32_t bsh = si.bsh, tail = si.tail_mask;
-    const uint32_t* __restrict__ masks_g = si.masks;
-    const uint4* sTQ1 = reinterpret_cast<const uint4*>(smem + si.o_TQ1);
-    const uint4* sD2 = reinterpret_cast<const uint4*>(smem + si.o_D2);
-    const uint4* sDQ2 = reinterpret_cast<const uint4*>(smem + si.o_DQ2);
-    const uint32_t* sDQ2w = reinterpret_cast<const uint32_t*>(sDQ2);
-    const uint32_t* sQ0 = reinterpret_cast<const uint32_t*>(smem + si.o_Q0);
-    const uint4* sBK = reinterpret_cast<const uint4*>(smem + si.o_BK);   // {slot, 3 keys}
-    const uint32_t* sK1 = reinterpret_cast<const uint32_t*>(smem + si.o_K1);
-    const uint32_t KM = si.km;
-    const uint64_t ob = item.o_begin, oe = item.o_end;
-    const uint64_t* list = item.list;
-    // word-mask: exactly F filters in the inner-ring stage (the host guarantees F <= filters and
-    // F <= tables built); scalar: a runtime count Feff <= F
-    uint32_t Feff = (uint32_t)F;
-    if (LAYOUT != ES_LAYOUT_WORDMASK) {
-        if (Feff > L.mask_filters) Feff = L.mask_filters;
-        if (Feff > nf) Feff = nf;
-    }
-    // residue stage: the next ES_NRES filters that carry 32-bit term residues
-    const uint32_t FR = min(si.F_built, Feff + ES_NRES) > Feff ? min(si.F_built, Feff + ES_NRES) : Feff;
-    TailCtx& C = Q->ctx;
-    if (lane == 0) {
-        C.M = M;
-        C.M_lo = si.M_lo;
-        C.kp1 = si.k + 1u;
-        C.M_big = (si.M_hi != 0) || (si.M_lo > C.kp1);
-        C.nf = nf;
-        C.r0 = si.r0;
-        C.tc = tcv;
-        C.allowed_g = si.allowed;
-        C.surv = L.surv;
-        C.surv_n = L.surv_n;
-        C.group_found = L.group_found;
-        C.surv_cap = L.surv_cap;
-        C.wcnt_saddr = wcnt_saddr;
-        C.item_id = item_id;
-        C.group = item.group;
-        C.t_blk = item.t;
-        C.Feff = Feff;
-        C.FR = FR;
-        C.r1 = si.r1;
-        C.strip = L.strip;
-        C.list = reinterpret_cast<const unsigned long long*>(item.list);
-        C.e_base = (item.list ? item.o_begin : item.c_begin) + (w - item.unit_begin) * 32ull * L.strip;
-    }
-    __syncwarp();
-    constexpr int FA = F > 0 ? F : 1;   // array extent
-    uint32_t qf[FA], corr[FA];
-    const uint32_t* tab[FA];
-#pragma unroll
-    for (int f = 0; f < F; ++f) {
-        const bool on = (uint32_t)f < Feff;
-        qf[f] = on ? sFC[f].q : 1u;
-        corr[f] = on ? sFC[f].corr : 0u;
-        tab[f] = LAYOUT == ES_LAYOUT_WORDMASK ? masks_g + si.mask_off[f] : si.allowed + (on ? sFC[f].off : 0u);
-    }
-    uint32_t cnt[FA];
-#pragma unroll
-    for (int f = 0; f < FA; ++f) cnt[f] = 0u;
-    uint32_t qhead = 0, qsize = 0;
-
-    const uint64_t rel = (w - item.unit_begin) * 32ull * L.strip + (uint64_t)lane * L.strip;
-    uint64_t e_lo, e_hi;
-    if (list) {
-        e_lo = ob + rel;
-        e_hi = e_lo + L.strip;
-        if (e_hi > oe) e_hi = oe;
-    } else {
-        e_lo = item.c_begin + rel;
-        e_hi = e_lo + L.strip;
-        if (e_hi > item.c_end) e_hi = item.c_end;
-    }
-    uint32_t d2 = 0;
-    uint32_t BQ2[FA];
-#pragma unroll
-    for (int f = 0; f < FA; ++f) BQ2[f] = 0u;
-    bool have = false;
-    uint64_t prev_c = 0;
-    // every lane runs L.strip steps so the warp-wide votes below see 32 lanes
-    for (uint32_t step = 0; step < L.strip; ++step) {
-        const uint64_t e = e_lo + step;
-        const bool live = e < e_hi;
-        if (__ballot_sync(0xffffffffu, live) == 0u) break;
-        uint64_t c = prev_c;
-        uint32_t lo1 = 0u, hi1 = 0u;
-        // b2 of the lane's last cycle lives in its record (0 before the first decode)
-        const U4 Mv = ldv_M(si);
-        U4 b2 = have ? ldv128(&Q->rec[lane][0]) : U4{0u, 0u, 0u, 0u};
-        if (live) {
-            if (list) {
-                const uint64_t o = __ldg(reinterpret_cast<const unsigned long long*>(list) + e);
-                c = o / r1;
-                lo1 = (uint32_t)(o - c * r1);
-                hi1 = lo1 + 1u;
-            } else {
-                c = e;
-                const uint64_t o0 = c * r1;
-                lo1 = ob > o0 ? (uint32_t)(ob - o0) : 0u;
-                const uint64_t span = oe - o0;
-                hi1 = span < r1 ? (uint32_t)span : r1;
-            }
-            // rings >= 2: one delta step while the ring-2 digit advances, else a decode
-            if (have && c == prev_c + 1 && d2 + 1u < r2) {
-                uint32_t wm;
-                b2 = addmod(b2, u4(sD2[d2]), Mv, wm);
-                uint32_t dq[8];
-                row8<F>(sDQ2 + d2 * (ES_FMAX / 4), dq);
-#pragma unroll
-                for (int f = 0; f < F; ++f) BQ2[f] = red2(BQ2[f] + dq[f] + (corr[f] & wm), qf[f]);
-                // this lane's record: b2 and the residue-stage residues, stepped the same way
-                const uint4 rq = Q->rec[lane][1];
-                uint32_t rv[ES_NRES] = {rq.x, rq.y, rq.z, rq.w};
-#pragma unroll
-                for (uint32_t j = 0; j < ES_NRES; ++j) {
-                    const uint32_t f = Feff + j;
-                    if (f < FR) rv[j] = red2(rv[j] + sDQ2w[d2 * ES_FMAX + f] + (sFC[f].corr & wm), sFC[f].q);
-                }
-                Q->rec[lane][0] = make_uint4(b2.x, b2.y, b2.z, b2.w);
-                Q->rec[lane][1] = make_uint4(rv[0], rv[1], rv[2], rv[3]);
-                ++d2;
-            } else if (!(have && c == prev_c)) {
-                b2 = decode_cycle(si, c, Mv, d2);
-#pragma unroll
-                for (int f = 0; f < F; ++f) {
-                    if ((uint32_t)f < Feff) BQ2[f] = red1(mod128(b2, sFC[f]) + tcv[f], qf[f]);
-                }
-                uint32_t rv[ES_NRES] = {0u, 0u, 0u, 0u};
-#pragma unroll
-                for (uint32_t j = 0; j < ES_NRES; ++j) {
-                    const uint32_t f = Feff + j;
-                    if (f < FR) rv[j] = red1(mod128(b2, sFC[f]) + tcv[f], sFC[f].q);
-                }
-                Q->rec[lane][0] = make_uint4(b2.x, b2.y, b2.z, b2.w);
-                Q->rec[lane][1] = make_uint4(rv[0], rv[1], rv[2], rv[3]);
-                have = true;
-            }
-            prev_c = c;
-        }
-        // A = M - b2 and its 32-bit key, once per ring-1 cycle
-        uint32_t brA;
-        const uint32_t KA = key32(sub128(Mv, b2, brA), ldv32(&si.sh));
-
-        // ---- ring 1: warp-uniform sweep (broadcast loads) --------------------------------
-        for (uint32_t d1 = 0; d1 < r1; ++d1) {
-            const bool act = (d1 - lo1) < (hi1 - lo1);          // lo1 <= d1 < hi1
-            // ring-1 wrap (b2 + T1 >= M, i.e. T1 >= A) from the 32-bit keys
-            const uint32_t k1 = sK1[d1];
-            uint32_t wm1 = k1 > KA ? 0xffffffffu : 0u;
-            uint32_t tq[8];
-            row8<F>(sTQ1 + d1 * (ES_FMAX / 4), tq);
-            // carry split of the inner ring: slots [split, r0) wrap past M.  Away from a key tie,
-            // t is the key of thr = M - b to within +-1 and fits 32 bits (0 <= t <= KM); keys
-            // below t-1 are certainly below thr, keys above t+1 certainly not.
-            const uint32_t t = wm1 ? KM - (k1 - KA) : KA - k1;
-            const uint32_t tl = max(t, 1u) - 1u;
-            const uint32_t th = min(t, 0xfffffffeu) + 1u;
-            // the bucket of tl holds its first slot and the next three keys (sorted): the split
-            // is that slot plus the keys below tl among the first two
-            const uint4 bk = sBK[tl >> bsh];
-            const bool s1 = bk.y < tl, s2 = bk.z < tl;
-            uint32_t split = bk.x + (s1 ? 1u : 0u) + (s2 ? 1u : 0u);
-            const uint32_t ks = s2 ? bk.w : (s1 ? bk.z : bk.y);   // key of slot `split`
-            // rare: a key tie with A, a key inside the +-1 band, or a crowded bucket -> exact
-            // (only lanes with candidates here: their record holds b2)
-            const bool rare = act && ((k1 == KA) || (ks <= th));
-            if (__any_sync(0xffffffffu, rare)) {
-                if (rare) {
-                    uint32_t wx, brw;
-                    const U4 Mr = ldv_M(si);
-                    const U4 b = addmod(ldv128(&Q->rec[lane][0]), ldv128(smem + ldv32(&si.o_T1) + 16u * d1), Mr, wx);
-                    wm1 = wx;
-                    const U4 thr = sub128(Mr, b, brw);
-                    const uint32_t te = key32(thr, ldv32(&si.sh));
-                    const uint32_t* rK0 = reinterpret_cast<const uint32_t*>(smem + ldv32(&si.o_K0));
-                    const uint4* rS0 = reinterpret_cast<const uint4*>(smem + ldv32(&si.o_S0));
-                    split = sBK[te >> bsh].x;
-                    while (rK0[split] < te) ++split;
-                    while (rK0[split] == te && lt128(u4(rS0[split]), thr)) ++split;   // S0[r0] = M stops it
-                }
-            }
-
-            if (LAYOUT == ES_LAYOUT_WORDMASK && WT == 2) {
-                // two inner words: both words of a phase are adjacent in P_f, so one 8-byte load
-                // per filter and phase serves them, and the pair is queued as one entry
-                uint32_t b0 = act ? 0xffffffffu : 0u, b1 = act ? tail : 0u;
-                const uint32_t cm0 = __funnelshift_lc(0u, 0xffffffffu, split);
-                const uint32_t cm1 = __funnelshift_lc(0u, 0xffffffffu, max(split, 32u) - 32u) & tail;
-#pragma unroll
-                for (int f = 0; f < F; ++f) {
-                    const uint32_t x0 = red2(BQ2[f] + tq[f] + (corr[f] & wm1), qf[f]);
-                    const uint32_t x1 = red1(x0 + corr[f], qf[f]);
-                    const uint2 m0 = __ldg(reinterpret_cast<const uint2*>(tab[f]) + x0);
-                    const uint2 m1 = __ldg(reinterpret_cast<const uint2*>(tab[f]) + x1);
-                    b0 &= (m0.x & ~cm0) | (m1.x & cm0);
-                    b1 &= (m0.y & ~cm1) | (m1.y & cm1);
-                    if (COUNT) cnt[f] += __popc(b0) + __popc(b1);
-                }
-                const uint32_t has = __ballot_sync(0xffffffffu, (b0 | b1) != 0u);
-                if (has) push<COUNT>(Q, smem, si, lane, step, qhead, qsize, has, b0, b1, split, d1, 0u, wm1);
-                continue;
-            }
-            uint32_t lo = 0u;   // bits of an even word, queued with the odd word after it
-            for (uint32_t wd = 0; wd < Wn; ++wd) {
-                const uint32_t valid = (wd + 1u == Wn) ? tail : 0xffffffffu;
-                uint32_t bits = act ? valid : 0u;
-                const uint32_t base = wd << 5;
-                // slots >= split of this word wrap: all-ones shifted left by (split - base) in [0, 32]
-                const uint32_t cm = __funnelshift_lc(0u, 0xffffffffu, max(split, base) - base) & valid;
-                if (LAYOUT == ES_LAYOUT_WORDMASK) {
-                    // straight-line cascade: two table loads per filter per 32 candidates
-#pragma unroll
-                    for (int f = 0; f < F; ++f) {
-                        const uint32_t x0 = red2(BQ2[f] + tq[f] + (corr[f] & wm1), qf[f]);   // n mod q_f, ring-0 base
-                        const uint32_t x1 = red1(x0 + corr[f], qf[f]);                      // the same after a wrap
-                        const uint32_t m0 = __ldg(tab[f] + x0 * Wn + wd);
-                        const uint32_t m1 = __ldg(tab[f] + x1 * Wn + wd);
-                        bits &= (m0 & ~cm) | (m1 & cm);
-                        if (COUNT) cnt[f] += __popc(bits);
-                    }
-                } else {
-                    bool alive = true;   // warp-uniform: some lane still has a live candidate
-#pragma unroll
-                    for (int f = 0; f < F; ++f) {
-                        if (alive && (uint32_t)f < Feff) {
-                            const uint32_t bqf = red2(BQ2[f] + tq[f] + (corr[f] & wm1), qf[f]);
-                            uint32_t nb = 0u, live_bits = bits;
-                            while (live_bits) {
-                                const uint32_t i = __ffs(live_bits) - 1u;
-                                live_bits &= live_bits - 1u;
-                                const uint32_t slot = base + i;
-                                const uint32_t m = red2(bqf + sQ0[f * r0 + slot] + ((slot >= split) ? corr[f] : 0u), qf[f]);
-                                const uint32_t wv = __ldg(tab[f] + (m >> 5));
-                                nb |= ((wv >> (m & 31u)) & 1u) << i;
-                            }
-                            bits = nb;
-                            if (COUNT) cnt[f] += __popc(bits);
-                            if (f + 1 < F && (uint32_t)(f + 1) < Feff) alive = __ballot_sync(0xffffffffu, bits != 0u) != 0u;
-                        }
-                    }
-                }
-                // ---- queue the survivors of the inner-ring stage -----------------------------
-                if ((wd & 1u) == 0u && wd + 1u < Wn) {
-                    lo = bits;
-                    continue;
-                }
-                const bool odd = (wd & 1u) != 0u;
-                const uint32_t plo = odd ? lo : bits, phi = odd ? bits : 0u;
-                const uint32_t has = __ballot_sync(0xffffffffu, (plo | phi) != 0u);
-                if (has) push<COUNT>(Q, smem, si, lane, step, qhead, qsize, has, plo, phi, split, d1, wd & ~1u, wm1);
-            }
-        }
-        // the records change with the next strip step: drain the queue
-        while (qsize) flush<COUNT>(Q, smem, si, lane, step, qhead, qsize);
-    }
-    // ---- per-stage counts of this warp-unit into the item's totals ----------------------
-    if (COUNT) {
-        unsigned long long* gc = item.counts;
-#pragma unroll
-        for (int f = 0; f < F; ++f) {
-            const uint32_t v = __reduce_add_sync(0xffffffffu, cnt[f]);
-            if (lane == 0 && v && gc && (uint32_t)f < Feff) atomicAdd(gc + f, (unsigned long long)v);
-        }
-        __syncwarp();
-        for (uint32_t f = Feff + lane; f < nf; f += 32u) {
-            const uint32_t v = wcnt[f];
-            if (v) {
-                if (gc) atomicAdd(gc + f, (unsigned long long)v);
-                wcnt[f] = 0u;
-            }
-        }
-        __syncwarp();
-    }
-}
-
-// Work distribution.  A warp-unit is 32 lanes x `strip` consecutive ring-1 cycles (or list
-// entries) of one item.  Direct mode (every item of the launch uses one plan): the CTA stages
-// the plan's tables once, then each warp claims warp-units from the global counter on its own --
-// no CTA barrier after staging.  Chunk mode (several plans): a CTA claims a chunk of
-// warp-units, restages when the plan changes, and its warps claim the chunk's units from a
-// shared counter; the only barriers are at chunk/item boundaries.
-//
-// Template: F = filters evaluated in the inner-ring stage (upper bound, runtime Feff <= F),
-// LAYOUT = word-mask or scalar tables, COUNT = per-stage pass counts, WT = words per inner ring
-// when known at compile time (1: r0 <= 32, 2: r0 <= 64), 0 = runtime.
-template <int F, int LAYOUT, bool COUNT, int WT>
-__global__ void __launch_bounds__(ES_LB_THREADS, ES_LB_MINB) es_scan_kernel(const __grid_constant__ EsLaunch L) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ EsInst si;
-    __shared__ unsigned long long s_u0, s_u1, s_end, s_next;
-    __shared__ uint32_t s_item;
-    __shared__ int s_skip;
-
-    const uint32_t tid = threadIdx.x;
-    const uint32_t lane = tid & 31u;
-    const uint32_t warp = tid >> 5;
-    EsQueue* Q = reinterpret_cast<EsQueue*>(smem + L.queue_off + warp * ES_QUEUE_BYTES);
-    uint32_t* wcnt = reinterpret_cast<uint32_t*>(smem + L.cnt_off) + warp * L.nf_max;
-    const uint32_t wcnt_saddr = (uint32_t)__cvta_generic_to_shared(wcnt);
-    const EsItem* items = L.items ? L.items : &L.item0;
-    const unsigned long long total = L.total_units;
-
-    if (COUNT)
-        for (uint32_t f = lane; f < L.nf_max; f += 32u) wcnt[f] = 0u;
-
-    if (L.direct) {
-        // ---- stage the one plan, then warps claim warp-units on their own ---------------
-        if (tid == 0) si = *items[0].inst;
-        __syncthreads();
-        copy_words(reinterpret_cast<uint32_t*>(smem), reinterpret_cast<const uint32_t*>(si.small), si.small_bytes >> 2);
-        __syncthreads();
-        for (;;) {
-            unsigned long long w = 0;
-            uint32_t it_id = 0;
-            int skip = 0;
-            if (lane == 0) {
-                w = atomicAdd(L.unit_counter, 1ull);
-                if (w < total) {
-                    uint32_t lo = 0, hi = L.n_items;
-                    while (hi - lo > 1) {
-                        const uint32_t mid = (lo + hi) >> 1;
-                        if (items[mid].unit_begin <= w) lo = mid; else hi = mid;
-                    }
-                    it_id = lo;
-                    if (L.group_found) {
-                        const unsigned long long fnd =
-                            *reinterpret_cast<volatile unsigned long long*>(L.group_found + items[lo].group);
-                        if (items[lo].t > fnd) skip = 1;
-                    }
-                }
-            }
-            w = __shfl_sync(0xffffffffu, w, 0);
-            if (w >= total) break;
-            it_id = __shfl_sync(0xffffffffu, it_id, 0);
-            skip = __shfl_sync(0xffffffffu, skip, 0);
-            if (skip) continue;
-            scan_unit<F, LAYOUT, COUNT, WT>(L, si, smem, Q, wcnt, wcnt_saddr, lane, w, items[it_id], it_id);
-        }
-        return;
-    }
-
-    uint32_t cur_inst = 0xffffffffu;
-    for (;;) {
-        // ---- CTA claims a chunk of warp-units; the size shrinks as the work runs out ---------
-        if (tid == 0) {
-            const unsigned long long cur = *reinterpret_cast<volatile unsigned long long*>(L.unit_counter);
-            const unsigned long long rem = cur < total ? total - cur : 0ull;
-            unsigned long long ch = rem / (2ull * gridDim.x);
-            if (ch < 1ull) ch = 1ull;
-            if (ch > (unsigned long long)L.chunk_max) ch = L.chunk_max;
-            const unsigned long long u0 = atomicAdd(L.unit_counter, ch);
-            s_u0 = u0;
-            s_u1 = (u0 + ch < total) ? u0 + ch : total;
-        }
-        __syncthreads();
-        const unsigned long long u1 = s_u1;
-        unsigned long long u = s_u0;
-        if (u >= total) break;
-        while (u < u1) {
-            if (tid == 0) {
-                uint32_t lo = 0, hi = L.n_items;
-                while (hi - lo > 1) {
-                    const uint32_t mid = (lo + hi) >> 1;
-                    if (items[mid].unit_begin <= u) lo = mid; else hi = mid;
-                }
-                const EsItem& it = items[lo];
-                unsigned long long e = it.unit_begin + it.n_units;
-                if (e > u1) e = u1;
-                int skip = 0;
-                if (L.group_found) {
-                    const unsigned long long fnd =
-                        *reinterpret_cast<volatile unsigned long long*>(L.group_found + it.group);
-                    if (it.t > fnd) skip = 1;
-                }
-                s_item = lo;
-                s_end = e;
-                s_next = u;
-                s_skip = skip;
-            }
-            __syncthreads();
-            const uint32_t item_id = s_item;
-            const unsigned long long end = s_end;
-            if (!s_skip) {
-                const EsItem& item = items[item_id];
-                if (item.inst_id != cur_inst) {
-                    // restage: the header, small tables and this plan's staged fast tables
-                    if (tid == 0) si = *item.inst;
-                    __syncthreads();
-                    copy_words(reinterpret_cast<uint32_t*>(smem), reinterpret_cast<const uint32_t*>(si.small),
-                               si.small_bytes >> 2);
-                    __syncthreads();
-                    cur_inst = item.inst_id;
-                }
-                for (;;) {
-                    unsigned long long w = 0;
-                    if (lane == 0) w = atomicAdd(&s_next, 1ull);
-                    w = __shfl_sync(0xffffffffu, w, 0);
-                    if (w >= end) break;
-                    scan_unit<F, LAYOUT, COUNT, WT>(L, si, smem, Q, wcnt, wcnt_saddr, lane, w, item, item_id);
-                }
-            }
-            __syncthreads();
-            u = end;
-        }
-    }
-}
 
 // Block-ordered minimum per search group: least (t, s) over good survivors.
 // out[g*4 + 0] = found, [1] = t, [2] = s_lo, [3] = s_hi.
@@ -837,39 +89,13 @@ __global__ void __launch_bounds__(256) es_int_peak_kernel(unsigned long long* si
     if (x == 0x9e3779b9u) atomicAdd(sink, 1ull);  // keeps the chains live
 }
 
-typedef void (*ScanFn)(const EsLaunch);
-
-template <bool COUNT, int WT>
-ScanFn pick_wm(uint32_t f) {
-    switch (f) {
-        case 0: return es_scan_kernel<0, ES_LAYOUT_WORDMASK, COUNT, WT>;
-        case 1: return es_scan_kernel<1, ES_LAYOUT_WORDMASK, COUNT, WT>;
-        case 2: return es_scan_kernel<2, ES_LAYOUT_WORDMASK, COUNT, WT>;
-        case 3: return es_scan_kernel<3, ES_LAYOUT_WORDMASK, COUNT, WT>;
-        case 4: return es_scan_kernel<4, ES_LAYOUT_WORDMASK, COUNT, WT>;
-        case 5: return es_scan_kernel<5, ES_LAYOUT_WORDMASK, COUNT, WT>;
-        case 6: return es_scan_kernel<6, ES_LAYOUT_WORDMASK, COUNT, WT>;
-        default: return es_scan_kernel<8, ES_LAYOUT_WORDMASK, COUNT, WT>;
-    }
-}
-
-template <bool COUNT>
-ScanFn pick_sc(uint32_t f) {
-    if (f <= 2) return es_scan_kernel<2, ES_LAYOUT_SCALAR, COUNT, 0>;
-    if (f <= 4) return es_scan_kernel<4, ES_LAYOUT_SCALAR, COUNT, 0>;
-    return es_scan_kernel<8, ES_LAYOUT_SCALAR, COUNT, 0>;
-}
-
-template <bool COUNT>
-ScanFn pick_w(int layout, uint32_t words, uint32_t f) {
-    if (layout == ES_LAYOUT_SCALAR) return pick_sc<COUNT>(f);
-    if (words == 1) return pick_wm<COUNT, 1>(f);
-    if (words == 2) return pick_wm<COUNT, 2>(f);
-    return pick_wm<COUNT, 0>(f);
-}
-
 ScanFn pick(int layout, int count, uint32_t words, uint32_t f) {
-    return count ? pick_w<true>(layout, words, f) : pick_w<false>(layout, words, f);
+    if (layout == ES_LAYOUT_SCALAR) return es_pick_scalar(count, f);
+    // pair tables exist for inner rings of one or two words.  words == 0 (a batch whose plans
+    // differ in width) and wider rings take the generic word-mask instance, which reads each
+    // plan's own width: a fixed-width instance would index past a narrower plan's tables.
+    if (layout == ES_LAYOUT_PAIR && (words == 1 || words == 2)) return es_pick_pair(count, words, f);
+    return es_pick_wordmask(count, words, f);
 }
 
 }  // namespace
@@ -878,11 +104,13 @@ ScanFn pick(int layout, int count, uint32_t words, uint32_t f) {
 int es_scan_prepare(int smem_optin_bytes) {
     const uint32_t fs[8] = {0, 1, 2, 3, 4, 5, 6, 8};
     const uint32_t ws[3] = {1, 2, 3};
-    for (int layout = 0; layout < 2; ++layout)
+    for (int layout = 0; layout < 3; ++layout)
         for (int count = 0; count < 2; ++count)
             for (uint32_t w : ws)
                 for (uint32_t f : fs) {
-                    cudaError_t e = cudaFuncSetAttribute(pick(layout, count, w, f),
+                    const ScanFn fn = pick(layout, count, w, f);
+                    if (!fn) return (int)cudaErrorInvalidDeviceFunction;
+                    cudaError_t e = cudaFuncSetAttribute(fn,
                                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                          smem_optin_bytes);
                     if (e != cudaSuccess) return (int)e;
@@ -892,12 +120,15 @@ int es_scan_prepare(int smem_optin_bytes) {
 
 int es_scan_occupancy(int layout, int count, uint32_t words, uint32_t mask_filters, int threads,
                       int smem_bytes, int* ctas_per_sm) {
-    return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        ctas_per_sm, pick(layout, count, words, mask_filters), threads, (size_t)smem_bytes);
+    const ScanFn fn = pick(layout, count, words, mask_filters);
+    if (!fn) return (int)cudaErrorInvalidDeviceFunction;
+    return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm, fn, threads, (size_t)smem_bytes);
 }
 
 int es_launch_scan(const EsLaunch& L, int layout, int count, uint32_t words, int grid, void* stream) {
-    pick(layout, count, words, L.mask_filters)<<<grid, L.threads, L.smem_bytes, (cudaStream_t)stream>>>(L);
+    const ScanFn fn = pick(layout, count, words, L.mask_filters);
+    if (!fn) return (int)cudaErrorInvalidDeviceFunction;
+    fn<<<grid, L.threads, L.smem_bytes, (cudaStream_t)stream>>>(L);
     return (int)cudaGetLastError();
 }
 

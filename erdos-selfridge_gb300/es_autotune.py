@@ -21,7 +21,7 @@ SPACE = {
     "threads": [256, 384, 512],
     "strip": [1, 2, 4],
     "mask_filters": [2, 3, 4, 5, 6],
-    "layout": [N.LAYOUT_WORDMASK, N.LAYOUT_SCALAR],
+    "layout": [N.LAYOUT_WORDMASK, N.LAYOUT_PAIR, N.LAYOUT_SCALAR],
 }
 DEFAULT = dict(layout=N.LAYOUT_WORDMASK, mask_filters=4, threads=512, strip=2, smem_kb=0,
                ctas_per_sm=4, count_stages=0)
@@ -74,12 +74,13 @@ def tune_plan(plan, ctx: N.Context | None = None, probe_log2: int = 28, cache: s
     if sig in data:
         return dict(data[sig]["tune"])
     own = ctx is None
+    start = dict(DEFAULT, layout=N.layout_for_plan(plan, DEFAULT["mask_filters"]))
     if own:
-        ctx = N.Context(plan, N.make_tune(**DEFAULT))
+        ctx = N.Context(plan, N.make_tune(**start))
     r0 = plan.radix[0] if plan.radix else 1
     n_outer = max(1, min(ctx.n_outer, (1 << probe_log2) // r0))
     ctx.set_block(0)
-    best = dict(DEFAULT)
+    best = dict(start)
     best_ms = time_ctx(ctx, best, n_outer)
     tried = {json.dumps(best, sort_keys=True): best_ms}
     space = space or SPACE
@@ -108,10 +109,12 @@ def tune_plan(plan, ctx: N.Context | None = None, probe_log2: int = 28, cache: s
     return best
 
 
-def tune_batch(ctxs, items, space: dict | None = None, reps: int = 3, log=None) -> tuple[dict, float]:
-    """Best shape for one persistent batch, timing the batch itself (graph replay)."""
+def tune_batch(ctxs, items, space: dict | None = None, reps: int = 3, log=None,
+               start: dict | None = None) -> tuple[dict, float]:
+    """Best shape for one persistent batch, timing the batch itself (graph replay), by coordinate
+    descent from `start` (DEFAULT when not given)."""
     space = space or SPACE
-    best, best_ms = dict(DEFAULT), None
+    best, best_ms = dict(start or DEFAULT), None
     tried = {}
 
     def run(t):

@@ -120,14 +120,20 @@ def batch64(seed: int = 0, autotune: bool = True, reps: int = 5, items_log2: int
 
 
 def k390(log2_positions: int = 40, filter_orders: dict | None = None, tune: dict | None = None,
-         reps: int = 1) -> dict:
-    """Both recorded wheels over [0, 2^log2_positions) of block 0 in one persistent launch."""
+         reps: int = 1, autotune: bool = False, tune_log2: int = 34) -> dict:
+    """Both recorded wheels over [0, 2^log2_positions) of block 0 in one persistent launch.  With
+    autotune the launch shape (inner-stage depth, layout, CTA size, strip) is chosen by the batch
+    autotuner on a 2^tune_log2-position prefix of each wheel first."""
     plans = {}
     for role, wheel in K390_WHEELS.items():
         order = (filter_orders or {}).get(role)
         plans[role] = es_gb300.Plan(390, None, wheel, filter_order=order)
-    t = dict(es_autotune.DEFAULT, **(tune or {}))
+    F = es_autotune.DEFAULT["mask_filters"]
+    t = dict(es_autotune.DEFAULT, layout=N.layout_for_plan(plans["primary"], F), **(tune or {}))
     ctxs = [N.Context(plans[r], N.make_tune(**t)) for r in ("primary", "confirmation")]
+    if autotune:
+        small = [(i, i, 0, 0, min(c.n_outer, -(-(1 << tune_log2) // c.r0))) for i, c in enumerate(ctxs)]
+        t, _ = es_autotune.tune_batch(ctxs, small, start=t)
     pos = 1 << log2_positions
     items = []
     for i, c in enumerate(ctxs):
@@ -171,20 +177,22 @@ def k390(log2_positions: int = 40, filter_orders: dict | None = None, tune: dict
             "cross_checked": True, "disagreements": disagree}
 
 
-def k390_learned(model_path: str, log2_positions: int = 40, reps: int = 2) -> dict:
+def k390_learned(model_path: str, log2_positions: int = 40, reps: int = 2, autotune: bool = True) -> dict:
     """The k = 390 fixed-scope confirmation scan with the learned cascade order of each wheel
-    against the same scan in the analytic (reference) order."""
+    against the same scan in the analytic (reference) order.  Both arms get the same engine
+    tuning: the batch autotuner picks each arm's launch shape for its own orders."""
     import es_learned
     model = es_learned.CostModel.load(model_path)
     orders, names = {}, {}
     for role, wheel in K390_WHEELS.items():
         P = es_gb300.Plan(390, None, wheel)
         names[role], orders[role] = es_learned.learned_order(model, P)
-    learned = k390(log2_positions, filter_orders=orders, reps=reps)
-    analytic = k390(log2_positions, reps=reps)
+    learned = k390(log2_positions, filter_orders=orders, reps=reps, autotune=autotune)
+    analytic = k390(log2_positions, reps=reps, autotune=autotune)
     same = all(learned["wheels"][r]["survivors_n"] == analytic["wheels"][r]["survivors_n"]
                for r in K390_WHEELS)
-    return {"learned_orders": names, "learned_ms": learned["ms"], "analytic_ms": analytic["ms"],
+    return {"learned_orders": names, "learned_tune": learned["tune"], "analytic_tune": analytic["tune"],
+            "learned_ms": learned["ms"], "analytic_ms": analytic["ms"],
             "learned_Gcand_s": learned["Gcand_s"], "analytic_Gcand_s": analytic["Gcand_s"],
             "wall_ratio_analytic_over_learned": analytic["ms"] / learned["ms"],
             "survivors_identical": same, "disagreements": learned["disagreements"] + analytic["disagreements"],
@@ -208,7 +216,7 @@ def main():
     elif a.which == "k390":
         out = k390(a.log2_positions)
     else:
-        out = k390_learned(a.model, a.log2_positions)
+        out = k390_learned(a.model, a.log2_positions, autotune=not a.no_autotune)
     s = json.dumps(out, default=str)
     if a.json:
         with open(a.json, "w") as f:

@@ -46,7 +46,7 @@ from es_plan import TUNABLES as _PLAN_TUNABLES  # noqa: E402
 TUNABLES = dict(_PLAN_TUNABLES)
 TUNABLES.update({
     "chunk_log2": 34,        # positions per _launch chunk issued by scan_block
-    "layout": "wordmask",    # "wordmask" | "scalar"
+    "layout": "auto",        # "auto" (pair or word-mask by table bytes) | "wordmask" | "pair" | "scalar"
     "threads": 512,          # CTA size
     "strip": 2,              # ring-1 cycles per lane per warp-unit
     "smem_kb": 0,            # shared-memory budget for staged word-mask tables (0: read via L1)
@@ -66,10 +66,14 @@ class Plan(_PlanBase):
         super().__init__(k, dict(TUNABLES, **(tun or {})), wheel, filter_order)
 
 
-def _tune_from(tun: dict) -> N.Tune:
-    layout = tun.get("layout", "wordmask")
-    return N.make_tune(layout=N.LAYOUT_SCALAR if layout == "scalar" else N.LAYOUT_WORDMASK,
-                       mask_filters=max(1, min(N.MAX_MASK_FILTERS, int(tun.get("fast_filters", 4)))),
+def _tune_from(tun: dict, plan=None) -> N.Tune:
+    layout = tun.get("layout", "auto")
+    F = max(1, min(N.MAX_MASK_FILTERS, int(tun.get("fast_filters", 4))))
+    if layout == "auto":
+        code = N.layout_for_plan(plan, F) if plan is not None else N.LAYOUT_WORDMASK
+    else:
+        code = {"scalar": N.LAYOUT_SCALAR, "pair": N.LAYOUT_PAIR}.get(layout, N.LAYOUT_WORDMASK)
+    return N.make_tune(layout=code, mask_filters=F,
                        threads=int(tun.get("threads", 512)), strip=int(tun.get("strip", 2)),
                        smem_kb=int(tun.get("smem_kb", 0)), ctas_per_sm=int(tun.get("ctas_per_sm", 4)),
                        count_stages=int(tun.get("count_stages", 0)))
@@ -164,7 +168,7 @@ class GpuSieve:
         self.tconst_h = np.zeros(max(1, self.nrest), dtype=np.uint32)
         self.r0 = P.radix[0] if P.radix else 1
         self.n_fast = max(0, min(int(P.tun.get("fast_filters", 4)), self.nrest))
-        self.tune = tune if tune is not None else _tune_from(P.tun)
+        self.tune = tune if tune is not None else _tune_from(P.tun, P)
         t0 = time.time()
         self.ctx = N.Context(P, self.tune, capacity=int(P.tun["max_survivors"]))
         self.compile_s = time.time() - t0          # table build + upload (no run-time compile)
@@ -176,7 +180,8 @@ class GpuSieve:
         self.ochunk = max(1, self.chunk // self.r0)
         self.launches = 0
         self.residues_checked = 0
-        self.mask_mode = "wordmask-gb300" if self.tune.layout == N.LAYOUT_WORDMASK else "scalar-gb300"
+        self.mask_mode = {N.LAYOUT_SCALAR: "scalar-gb300", N.LAYOUT_PAIR: "pair-gb300"}.get(
+            self.tune.layout, "wordmask-gb300")
         self.tconst = _Tconst(self)
         self.out_n = _OutN(self)
         self.out = _Out(self)

@@ -191,7 +191,8 @@ WHEEL_TUNES = [
 
 def _orders(plan, rng, shuffles: int = 2) -> list[tuple[str, list[int]]]:
     """Cascade-order families: the reference order, orders that trade rejection against the
-    word-mask table footprint (several L1 budgets), small-q-first heads, and random heads."""
+    word-mask table footprint (several L1 budgets, two of them sized for pair tables),
+    small-q-first heads, and random heads."""
     ref = list(plan.rest)
     out = [("reference", ref)]
     W = ((plan.radix[0] if plan.radix else 1) + 31) // 32
@@ -205,8 +206,10 @@ def _orders(plan, rng, shuffles: int = 2) -> list[tuple[str, list[int]]]:
     for name, scale in (("table-aware-16k", 16384.0), ("table-aware", 65536.0), ("table-aware-256k", 262144.0)):
         head = sorted(ref, key=lambda p: (1.0 - rates[p]) / (1.0 + size[p] / scale), reverse=True)[:N_FIRST]
         out.append((name, rest_after(head)))
-    # greedy: most rejection among the first four within an L1 budget, the rest by pass rate
-    for name, budget in (("l1-96k", 96 * 1024), ("l1-160k", 160 * 1024)):
+    # greedy: most rejection among the first four within an L1 budget, the rest by pass rate; the
+    # two smallest budgets keep the pair tables (twice the bytes, one load per filter) in L1 too
+    for name, budget in (("l1-96k", 96 * 1024), ("l1-160k", 160 * 1024), ("l1-pair-48k", 48 * 1024),
+                         ("l1-pair-88k", 88 * 1024)):
         head, used = [], 0
         for p in sorted(ref, key=lambda p: rates[p]):
             if len(head) < 4 and used + size[p] <= budget:
@@ -275,7 +278,10 @@ def probe(item: dict, tune=None, log2_pos: int | None = None, reps: int = 3) -> 
     log2_pos = PROBE_LOG2 if log2_pos is None else log2_pos
     k, radix, lo, hi, q, allowed, M = item["arrays"]
     A = N.PlanArrays.from_arrays(k, radix, lo, hi, q, allowed, M)
-    t = N.make_tune(**dict(tune or {}, count_stages=1))
+    tune = dict(tune or {})
+    if "layout" not in tune:   # the engine's default choice for this plan
+        tune["layout"] = N.layout_for(int(radix[0]) if len(radix) else 1, q, tune.get("mask_filters", 4))
+    t = N.make_tune(**dict(tune, count_stages=1))
     ctx = N.Context.from_arrays(A, t, len(q))
     try:
         r0 = int(radix[0]) if len(radix) and radix[0] else 1
@@ -285,7 +291,7 @@ def probe(item: dict, tune=None, log2_pos: int | None = None, reps: int = 3) -> 
         ctx.reset()
         ctx.launch(0, n_outer)
         counts = [int(x) for x in ctx.stage_counts()]
-        ctx.set_tune(N.make_tune(**dict(tune or {}, count_stages=0)))
+        ctx.set_tune(N.make_tune(**dict(tune, count_stages=0)))
         ctx.reset()
         ctx.launch_timed(0, n_outer)
         ms = []

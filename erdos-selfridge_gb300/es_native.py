@@ -19,6 +19,7 @@ ES_OK = 0
 ES_ERR_OVERFLOW = -3
 LAYOUT_WORDMASK = 0
 LAYOUT_SCALAR = 1
+LAYOUT_PAIR = 2       # word masks with the wrapped row beside each phase (inner rings <= 64 slots)
 MAX_MASK_FILTERS = 8
 
 
@@ -173,6 +174,31 @@ class PlanArrays:
                              radix=_ptr(self.radix, C.c_uint32), term_lo=_ptr(self.term_lo, C.c_uint64),
                              term_hi=_ptr(self.term_hi, C.c_uint64), filter_q=_ptr(self.q, C.c_uint32),
                              allowed=_ptr(self.allowed, C.c_uint32))
+
+
+# L1 bytes the phase tables can count on beside the scan's ~51 KB of shared memory (each SM has
+# 256 KB for L1 and shared memory together; the driver's carveout for the scan is 64 KB)
+L1_TABLE_BUDGET = 180 * 1024
+
+
+def layout_for(r0: int, filter_q, mask_filters: int) -> int:
+    """Table layout of the inner-ring stage for an inner ring of r0 slots whose first filters have
+    moduli filter_q.  Pair tables cost one load per filter and word instead of two, but twice the
+    bytes: they win unless the word-mask tables fit L1 and the pair tables do not (measured on
+    GB300: k = 300 keeps word masks at F = 3..4, k = 390 gains about 1.3x from pairs).  Neither
+    choice changes which candidates pass."""
+    W = -(-max(1, int(r0)) // 32)
+    if W > 2:
+        return LAYOUT_WORDMASK
+    qs = [int(q) for q in list(filter_q)[:min(int(mask_filters), MAX_MASK_FILTERS)]]
+    single = 4 * sum(-(-(q * W) // 4) * 4 for q in qs)
+    if single <= L1_TABLE_BUDGET < 2 * single:
+        return LAYOUT_WORDMASK
+    return LAYOUT_PAIR
+
+
+def layout_for_plan(plan, mask_filters: int) -> int:
+    return layout_for(plan.radix[0] if plan.radix else 1, [plan.info[p][0] for p in plan.rest], mask_filters)
 
 
 def make_tune(layout=LAYOUT_WORDMASK, mask_filters=4, threads=512, strip=2, smem_kb=0,

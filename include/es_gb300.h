@@ -39,6 +39,9 @@ extern "C" {
 
 #define ES_LAYOUT_WORDMASK 0  /* phase word-mask tables: 32 candidates per load */
 #define ES_LAYOUT_SCALAR 1    /* per-candidate incremental residue + bit-table test */
+#define ES_LAYOUT_PAIR 2      /* word-mask tables with each phase's wrapped row beside it: one
+                                 load per filter and word (inner rings of <= 64 slots; wider
+                                 rings use ES_LAYOUT_WORDMASK) */
 
 #define ES_MAX_MASK_FILTERS 8 /* filters evaluated in the inner-ring stage */
 #define ES_MAX_Q (1u << 20)   /* filter moduli q = p^t_p must be below 2^20 (k <= 1024) */
@@ -70,7 +73,7 @@ typedef struct es_plan_desc {
 /* Launch shape and table layout; chosen by the autotuner (es_autotune.py).  None of these
  * changes which candidates pass. */
 typedef struct es_tune {
-    uint32_t layout;        /* ES_LAYOUT_WORDMASK or ES_LAYOUT_SCALAR */
+    uint32_t layout;        /* ES_LAYOUT_WORDMASK, ES_LAYOUT_SCALAR or ES_LAYOUT_PAIR */
     uint32_t mask_filters;  /* filters in the inner-ring stage, 1..ES_MAX_MASK_FILTERS */
     uint32_t threads;       /* CTA size, multiple of 32 in [64, 512] */
     uint32_t strip;         /* ring-1 cycles per thread per work unit (strip depth) */

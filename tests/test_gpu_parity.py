@@ -21,6 +21,8 @@ SHAPES = [
     dict(layout=0, mask_filters=2, threads=512, strip=7, smem_kb=0),
     dict(layout=1, mask_filters=4, threads=256, strip=3),
     dict(layout=1, mask_filters=6, threads=96, strip=2, smem_kb=16),
+    dict(layout=2, mask_filters=4, threads=256, strip=2),
+    dict(layout=2, mask_filters=3, threads=512, strip=5),
 ]
 
 
@@ -67,7 +69,7 @@ def test_k300_seeded_sample(native):
     plan = es_gb300.Plan(300)
     assert [[p, T] for p, T in plan.wheel] == g["plan"]["wheel"]
     outer = _sample(g["seed"], g["domain"], g["draws"], g["outer_sha256"])
-    for shape in (SHAPES[0], SHAPES[3], dict(layout=0, mask_filters=8, threads=512, strip=16)):
+    for shape in (SHAPES[0], SHAPES[3], SHAPES[5], dict(layout=0, mask_filters=8, threads=512, strip=16)):
         ctx = N.Context(plan, _tune(N, **shape))
         ctx.set_block(0)
         ctx.reset()
@@ -87,13 +89,15 @@ def test_k390_seeded_sample(native, role):
     plan = es_gb300.Plan(390, None, g["wheel"])
     assert str(plan.M) == g["plan"]["M"] and plan.rest == g["plan"]["rest"]
     outer = _sample(g["seed"], g["domain"], g["draws"], g["outer_sha256"])
-    ctx = N.Context(plan, _tune(N, mask_filters=8))
-    ctx.set_block(0)
-    ctx.reset()
-    ctx.reset_counts()
-    ctx.launch_list(outer)
-    assert sorted(int(x) for x in ctx.survivors()) == g["survivors"]
-    assert [int(x) for x in ctx.stage_counts()] == g["counts"]
+    for shape in (dict(mask_filters=8), dict(layout=2, mask_filters=4), dict(layout=2, mask_filters=3, strip=1)):
+        ctx = N.Context(plan, _tune(N, **shape))
+        ctx.set_block(0)
+        ctx.reset()
+        ctx.reset_counts()
+        ctx.launch_list(outer)
+        assert sorted(int(x) for x in ctx.survivors()) == g["survivors"], shape
+        assert [int(x) for x in ctx.stage_counts()] == g["counts"], shape
+        ctx.close()
 
 
 def test_k300_chunk_additivity_and_oracle(native):
@@ -132,8 +136,9 @@ def test_batch64_prefixes(native):
         assert [[p, T] for p, T in plan.wheel] == inst["plan"]["wheel"]
         ctxs.append(N.Context(plan, _tune(N)))
         items.append((i, i, 0, 0, inst["prefix_outer"]))
-    for graph in (False, True):
-        b = N.Batch(ctxs, items, _tune(N, mask_filters=6, strip=2))
+    # the plans differ in inner-ring width, so the pair layout runs the generic word-mask instance
+    for graph, layout in ((False, 0), (True, 0), (False, 2)):
+        b = N.Batch(ctxs, items, _tune(N, layout=layout, mask_filters=6, strip=2))
         b.run(use_graph=graph)
         b.sync()
         surv = b.survivors()

@@ -127,3 +127,22 @@ def test_load_known(tmp_path):
     b.write_text("2 99\n3 7\n")
     known = es_gb300.load_known(str(a), str(b), str(tmp_path / "missing.txt"))
     assert known == {1: (3, "a.txt"), 2: (6, "a.txt"), 3: (7, "b.txt")}
+
+
+def test_layout_rule():
+    """The default table layout: word masks where they fit L1 and pair tables would not (k = 300
+    at F = 3..4), pair tables where neither fits (k = 390) or both fit, word masks for inner rings
+    wider than two words; "auto" in the drop-in tunables resolves through it."""
+    import es_gb300
+    import es_native as N
+    P300 = es_gb300.Plan(300)
+    assert N.layout_for_plan(P300, 4) == N.LAYOUT_WORDMASK
+    assert N.layout_for_plan(P300, 3) == N.LAYOUT_WORDMASK
+    assert N.layout_for_plan(P300, 5) == N.LAYOUT_PAIR
+    assert N.layout_for_plan(P300, 2) == N.LAYOUT_PAIR
+    wheel = [[3, 6], [2, 9], [211, 1], [139, 1], [103, 1], [137, 1], [101, 1], [67, 1], [5, 2],
+             [199, 1], [23, 2], [79, 1], [197, 1], [131, 1], [7, 2], [17, 1]]
+    assert N.layout_for_plan(es_gb300.Plan(390, None, wheel), 4) == N.LAYOUT_PAIR
+    assert N.layout_for(96, [1009, 1013], 2) == N.LAYOUT_WORDMASK
+    assert es_gb300._tune_from(dict(es_gb300.TUNABLES), P300).layout == N.LAYOUT_WORDMASK
+    assert es_gb300._tune_from(dict(es_gb300.TUNABLES, layout="scalar"), P300).layout == N.LAYOUT_SCALAR
