@@ -347,7 +347,10 @@ def main():
         import es_learned
         model = es_learned.CostModel.load(es_learned.MODEL_PATH)
         oname, order = es_learned.learned_order(model, plan)
-        lctx = N.Context(plan.with_order(order), sieve.tune)
+        lplan = plan.with_order(order)
+        ltune = N.make_tune(**dict(N.tune_dict(sieve.tune),
+                                   layout=N.layout_for_plan(lplan, sieve.tune.mask_filters)))
+        lctx = N.Context(lplan, ltune)
         lctx.set_block(0)
         for _ in range(3):
             lctx.reset()
