@@ -411,9 +411,12 @@ int es_ctx_create(const es_plan_desc* d, const es_tune* tune_in, es_ctx** out) {
     if (nf) memcpy(&small[I.o_FC], fc.data(), sizeof(EsFilterC) * nf);
 
     // ---- word-mask phase tables for the first FB filters ---------------------------------
+    // rows of RS words: W, except three-word rings, whose rows are padded to four words so that
+    // one 16-byte load reads a row
+    const uint32_t RS = W == 3 ? 4u : W;
     std::vector<uint32_t> mask_off(ES_FMAX + 1, 0);
     for (uint32_t f = 0; f < ES_FMAX; ++f)
-        mask_off[f + 1] = mask_off[f] + (f < FB ? (uint32_t)align_up((uint64_t)c->q[f] * W, 4) : 0u);
+        mask_off[f + 1] = mask_off[f] + (f < FB ? (uint32_t)align_up((uint64_t)c->q[f] * RS, 4) : 0u);
     std::vector<uint32_t> masks(std::max<uint32_t>(mask_off[ES_FMAX], 4), 0u);
     for (uint32_t f = 0; f < FB; ++f) {
         const uint32_t q = c->q[f];
@@ -423,7 +426,7 @@ int es_ctx_create(const es_plan_desc* d, const es_tune* tune_in, es_ctx** out) {
             const uint32_t wd = i >> 5, bit = 1u << (i & 31u);
             uint32_t r = a;
             for (uint32_t ph = 0; ph < q; ++ph) {
-                if (admissible(f, r)) P[(uint64_t)ph * W + wd] |= bit;
+                if (admissible(f, r)) P[(uint64_t)ph * RS + wd] |= bit;
                 if (++r == q) r = 0;
             }
         }
@@ -491,6 +494,7 @@ int es_ctx_create(const es_plan_desc* d, const es_tune* tune_in, es_ctx** out) {
     I.km = (uint32_t)(M >> sh);
     I.small_bytes = (uint32_t)small_bytes;
     for (uint32_t f = 0; f <= ES_FMAX; ++f) I.mask_off[f] = mask_off[f];
+    I.mask_stride = RS;
     I.small = c->d_arena + a_small;
     I.masks = reinterpret_cast<const uint32_t*>(c->d_arena + a_masks);
     I.pairs = reinterpret_cast<const uint32_t*>(c->d_arena + a_pairs);

@@ -16,7 +16,8 @@
 //                               the next two keys                            16 B each
 //                   FC[nf]      per-filter constants (EsFilterC)             32 B each
 //   fast tables   for the first F_built filters: word-mask phase tables
-//                   P_f[phi][w] bit i = admissible((phi + S0[32w+i]) mod q_f), q_f x W words
+//                   P_f[phi][w] bit i = admissible((phi + S0[32w+i]) mod q_f), q_f rows of
+//                   mask_stride words (W, or 4 for W = 3: padded to one 16-byte load)
 //   bit tables    every filter's packed admissible-residue bits (ceil(q/32) words)
 //   ring terms    all rings' 128-bit terms (decode of rings >= 2 at strip starts)
 #pragma once
@@ -57,7 +58,7 @@ struct EsInst {
     uint32_t o_T1, o_TQ1, o_D2, o_DQ2, o_S0, o_K0, o_I0, o_Q0, o_BK, o_FC, o_K1;
     // word offsets of the fast (word-mask) tables, F_built + 1 entries (prefix sums)
     uint32_t mask_off[ES_FMAX + 1];
-    uint32_t pad0;
+    uint32_t mask_stride;            // words per phase row of P_f: W, or 4 for W = 3 (16-byte rows)
     const unsigned char* small;      // device copy of the small block
     const uint32_t* masks;           // word-mask tables
     const uint32_t* pairs;           // pair tables (W <= 2): row phi = P_f[phi], P_f[(phi + corr_f) mod q_f]
@@ -110,9 +111,10 @@ struct EsLaunch {
     uint32_t tconst0[ES_MAX_FILTERS];
 };
 
-// Scan kernel instances by layout (es_scan_wm.cu, es_scan_pair.cu, es_scan_sc.cu).
+// Scan kernel instances by layout (es_scan_wm.cu / es_scan_wmc.cu, es_scan_pair.cu, es_scan_sc.cu).
 typedef void (*ScanFn)(const EsLaunch);
-ScanFn es_pick_wordmask(int count, uint32_t words, uint32_t mask_filters);
+ScanFn es_pick_wordmask_fast(uint32_t words, uint32_t mask_filters);
+ScanFn es_pick_wordmask_count(uint32_t words, uint32_t mask_filters);
 ScanFn es_pick_pair(int count, uint32_t words, uint32_t mask_filters);
 ScanFn es_pick_scalar(int count, uint32_t mask_filters);
 

@@ -1,6 +1,7 @@
 // Dispatch of the scan kernel instances, the block-ordered min-reduction and the integer-pipe
 // peak probe of the GB300 Erdős–Selfridge CRT-wheel sieve (sm_103a).  The scan kernel itself is
-// es_scan_kernel.cuh, instantiated per layout in es_scan_wm.cu, es_scan_pair.cu, es_scan_sc.cu.
+// es_scan_kernel.cuh, instantiated per layout in es_scan_wm.cu / es_scan_wmc.cu (word masks,
+// production and counting launches), es_scan_pair.cu and es_scan_sc.cu.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -95,7 +96,7 @@ ScanFn pick(int layout, int count, uint32_t words, uint32_t f) {
     // differ in width) and wider rings take the generic word-mask instance, which reads each
     // plan's own width: a fixed-width instance would index past a narrower plan's tables.
     if (layout == ES_LAYOUT_PAIR && (words == 1 || words == 2)) return es_pick_pair(count, words, f);
-    return es_pick_wordmask(count, words, f);
+    return count ? es_pick_wordmask_count(words, f) : es_pick_wordmask_fast(words, f);
 }
 
 }  // namespace
@@ -103,7 +104,7 @@ ScanFn pick(int layout, int count, uint32_t words, uint32_t f) {
 // Raise the dynamic shared-memory limit of every scan instance once per process/device.
 int es_scan_prepare(int smem_optin_bytes) {
     const uint32_t fs[8] = {0, 1, 2, 3, 4, 5, 6, 8};
-    const uint32_t ws[3] = {1, 2, 3};
+    const uint32_t ws[4] = {1, 2, 3, 5};   // every word-count instance: 1, 2, 3-4, generic
     for (int layout = 0; layout < 3; ++layout)
         for (int count = 0; count < 2; ++count)
             for (uint32_t w : ws)

@@ -1,5 +1,5 @@
 // The scan kernel of the GB300 Erdős–Selfridge CRT-wheel sieve (sm_103a), as a template that
-// es_scan_wm.cu, es_scan_pair.cu and es_scan_sc.cu instantiate (one layout each, compiled in
+// es_scan_wm.cu / es_scan_wmc.cu, es_scan_pair.cu and es_scan_sc.cu instantiate (compiled in
 // parallel); es_scan.cu holds the dispatch, the min-reduction and the peak probe.
 //
 // What one launch computes (semantics of the reference kernel, sieve/gpu_sieve_v9.py:240-330,
@@ -352,7 +352,9 @@ __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, u
     const uint32_t* tcv = L.items ? item.tconst : L.tconst0;
     const uint32_t nf = si.n_filters;
     const uint32_t r0 = si.r0, r1 = si.r1, r2 = si.r2;
-    const uint32_t Wn = WT ? (uint32_t)WT : si.W;
+    // words per inner ring (WT = 4 serves rings of three and four words) and per phase-table row
+    const uint32_t Wn = (WT == 1 || WT == 2) ? (uint32_t)WT : si.W;
+    const uint32_t RSn = (WT == 1 || WT == 2) ? (uint32_t)WT : (WT == 4 ? 4u : si.mask_stride);
     const uint32_t bsh = si.bsh, tail = si.tail_mask;
     const uint32_t* __restrict__ masks_g = si.masks;
     const uint4* sTQ1 = reinterpret_cast<const uint4*>(smem + si.o_TQ1);
@@ -560,6 +562,34 @@ __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, u
                 if (has) push<COUNT>(Q, smem, si, lane, step, qhead, qsize, has, b0, b1, split, d1, 0u, wm1);
                 continue;
             }
+            if (LAYOUT == ES_LAYOUT_WORDMASK && WT == 4) {
+                // three or four inner words: rows padded to four words, so each side of the
+                // carry split is one 16-byte load per filter; two pair entries per outer index
+                uint32_t b[4], cmw[4];
+#pragma unroll
+                for (uint32_t w = 0; w < 4; ++w) {
+                    const uint32_t valid = w + 1u < Wn ? 0xffffffffu : (w + 1u == Wn ? tail : 0u);
+                    b[w] = act ? valid : 0u;
+                    cmw[w] = __funnelshift_lc(0u, 0xffffffffu, max(split, 32u * w) - 32u * w) & valid;
+                }
+#pragma unroll
+                for (int f = 0; f < F; ++f) {
+                    const uint32_t x0 = red2(BQ2[f] + tq[f] + (corr[f] & wm1), qf[f]);
+                    const uint32_t x1 = red1(x0 + corr[f], qf[f]);
+                    const uint4 m0 = __ldg(reinterpret_cast<const uint4*>(tab[f]) + x0);
+                    const uint4 m1 = __ldg(reinterpret_cast<const uint4*>(tab[f]) + x1);
+                    b[0] &= (m0.x & ~cmw[0]) | (m1.x & cmw[0]);
+                    b[1] &= (m0.y & ~cmw[1]) | (m1.y & cmw[1]);
+                    b[2] &= (m0.z & ~cmw[2]) | (m1.z & cmw[2]);
+                    b[3] &= (m0.w & ~cmw[3]) | (m1.w & cmw[3]);
+                    if (COUNT) cnt[f] += __popc(b[0]) + __popc(b[1]) + __popc(b[2]) + __popc(b[3]);
+                }
+                const uint32_t h0 = __ballot_sync(0xffffffffu, (b[0] | b[1]) != 0u);
+                if (h0) push<COUNT>(Q, smem, si, lane, step, qhead, qsize, h0, b[0], b[1], split, d1, 0u, wm1);
+                const uint32_t h1 = __ballot_sync(0xffffffffu, (b[2] | b[3]) != 0u);
+                if (h1) push<COUNT>(Q, smem, si, lane, step, qhead, qsize, h1, b[2], b[3], split, d1, 2u, wm1);
+                continue;
+            }
             if (LAYOUT == ES_LAYOUT_WORDMASK && WT == 2) {
                 // two inner words: both words of a phase are adjacent in P_f, so one 8-byte load
                 // per filter and phase serves them, and the pair is queued as one entry
@@ -593,8 +623,8 @@ __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, u
                     for (int f = 0; f < F; ++f) {
                         const uint32_t x0 = red2(BQ2[f] + tq[f] + (corr[f] & wm1), qf[f]);   // n mod q_f, ring-0 base
                         const uint32_t x1 = red1(x0 + corr[f], qf[f]);                      // the same after a wrap
-                        const uint32_t m0 = __ldg(tab[f] + x0 * Wn + wd);
-                        const uint32_t m1 = __ldg(tab[f] + x1 * Wn + wd);
+                        const uint32_t m0 = __ldg(tab[f] + x0 * RSn + wd);
+                        const uint32_t m1 = __ldg(tab[f] + x1 * RSn + wd);
                         bits &= (m0 & ~cm) | (m1 & cm);
                         if (COUNT) cnt[f] += __popc(bits);
                     }
@@ -662,7 +692,8 @@ __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, u
 //
 // Template: F = filters evaluated in the inner-ring stage (upper bound, runtime Feff <= F),
 // LAYOUT = word-mask or scalar tables, COUNT = per-stage pass counts, WT = words per inner ring
-// when known at compile time (1: r0 <= 32, 2: r0 <= 64), 0 = runtime.
+// when known at compile time (1: r0 <= 32, 2: r0 <= 64, 4: r0 <= 128, rows of four words),
+// 0 = runtime.
 template <int F, int LAYOUT, bool COUNT, int WT>
 __global__ void __launch_bounds__(ES_LB_THREADS, ES_LB_MINB) es_scan_kernel(const __grid_constant__ EsLaunch L) {
     extern __shared__ __align__(16) unsigned char smem[];

@@ -10,6 +10,8 @@
 * batch64: 64 seeded instances (k uniform in 150..400, range lengths log-uniform in 2^20..2^32
   positions of block 0, each with its own planner wheel) in ONE persistent work-stealing launch
   replayed from a CUDA graph, launch shape from the autotuner, against one launch per instance.
+* replay: whole blocks of recorded frontier wheels (k = 378..400), each compared with the
+  reference driver's recorded audit record (survivor counts and sha256 of the survivors).
 * k390: the two recorded k = 390 wheels (primary and confirmation of evidence/through400/
   runs.json) over positions [0, 2^40) of block 0 in one persistent launch; every survivor of
   either wheel that the other wheel's scanned prefix covers must be a survivor there too.
@@ -199,9 +201,37 @@ def k390_learned(model_path: str, log2_positions: int = 40, reps: int = 2, autot
             "learned": learned, "analytic": analytic}
 
 
+AUDIT_FIELDS = ("residues_enumerated", "kernel_survivors", "after_n_gt_k_plus_1", "passed_ref_is_good",
+                "sha256_survivors")
+
+
+def replay(cases, chunk_log2: int = 40) -> dict:
+    """Whole-block replays of recorded frontier wheels: every position of block t through the
+    drop-in scan_block, then the reference driver's audit record (counts and survivor hash),
+    compared field by field with the recorded one."""
+    out = []
+    for c in cases:
+        plan = es_gb300.Plan(c["k"], {"chunk_log2": chunk_log2}, c["wheel"])
+        assert str(plan.M) == str(c["M"]) and plan.R == int(c["R"]), "wheel does not rebuild"
+        sieve = es_gb300.GpuSieve(plan)
+        t = int(c["audit"]["t"])
+        t0 = time.perf_counter()
+        idx = sieve.scan_block(t)
+        wall = time.perf_counter() - t0
+        audit = es_gb300.block_audit(plan, t, idx)
+        same = {f: audit[f] == c["audit"][f] for f in AUDIT_FIELDS}
+        out.append({"k": c["k"], "role": c["role"], "t": t, "R": plan.R, "wall_s": wall,
+                    "Gcand_s": plan.R / wall / 1e9, "mask_mode": sieve.mask_mode,
+                    "audit": audit, "matches_record": all(same.values()), "fields": same})
+    return {"cases": out, "all_match": all(x["matches_record"] for x in out),
+            "positions": sum(x["R"] for x in out), "wall_s": sum(x["wall_s"] for x in out)}
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("which", choices=["small-k", "batch64", "k390", "k390-learned"])
+    ap.add_argument("which", choices=["small-k", "batch64", "k390", "k390-learned", "replay"])
+    ap.add_argument("--cases-file", default=None, help="recorded block audits (replay), JSON {cases: [...]}")
+    ap.add_argument("--select", default=None, help="replay: comma list of k:role:t to run")
     ap.add_argument("--model", default=None, help="learned cost model (es_learned.py --save-model)")
     ap.add_argument("--json", default=None)
     ap.add_argument("--bfile", default=None)
@@ -215,8 +245,14 @@ def main():
         out = batch64(autotune=not a.no_autotune)
     elif a.which == "k390":
         out = k390(a.log2_positions)
-    else:
+    elif a.which == "k390-learned":
         out = k390_learned(a.model, a.log2_positions, autotune=not a.no_autotune)
+    else:
+        cases = json.load(open(a.cases_file))["cases"]
+        if a.select:
+            want = set(a.select.split(","))
+            cases = [c for c in cases if f"{c['k']}:{c['role']}:{c['audit']['t']}" in want]
+        out = replay(cases)
     s = json.dumps(out, default=str)
     if a.json:
         with open(a.json, "w") as f:

@@ -21,6 +21,7 @@ Kummer test, as the reference does with its frozen referee (sieve/gpu_sieve_v9.p
 from __future__ import annotations
 
 import argparse
+import hashlib
 import json
 import math
 import os
@@ -108,6 +109,24 @@ def verdict(plan, t: int, surv) -> tuple[list[int], list[int], list[int]]:
     gs = set(good)
     bad = [n for n in cands if n > plan.k + 1 and n not in gs]
     return cands, good, bad
+
+
+def survivor_hash(ns) -> str:
+    """A block's survivor hash, reproducible by a third party (harness/run_k.py:38-44): sha256 of
+    the UTF-8 bytes of the sorted decimal n joined by newlines, no trailing newline."""
+    return hashlib.sha256("\n".join(str(int(n)) for n in sorted(ns)).encode()).hexdigest()
+
+
+def block_audit(plan, t: int, surv) -> dict:
+    """The per-block audit record the reference driver keeps (harness/run_k.py:145-158), from a
+    block's kernel survivors (position indices): counts before and after n > k + 1 and the exact
+    test, the survivors when there are few, and their hash."""
+    cands, good, _ = verdict(plan, t, surv)
+    return {"t": int(t), "residues_enumerated": plan.R, "kernel_survivors": len(cands),
+            "after_n_gt_k_plus_1": sum(1 for n in cands if n > plan.k + 1),
+            "passed_ref_is_good": len(good),
+            "survivors_n": [str(n) for n in cands] if len(cands) <= 64 else None,
+            "sha256_survivors": survivor_hash(cands)}
 
 
 class _Tconst:

@@ -265,6 +265,25 @@ def main() -> None:
         json.dump(out, open(os.path.join(HERE, "scan_k390_sample.json"), "w"))
         print("k390", time.time() - t0, file=sys.stderr)
 
+    if want("replay"):
+        # the recorded full-block audits of the frontier wheels (harness/run_k.py:145-158 fields),
+        # for whole-block replays: every role/block of k = 378..400 with its R and survivor hash
+        runs = json.load(open(os.path.join(ref_root, "evidence", "through400", "runs.json")))["terms"]
+        cases = []
+        for term in runs:
+            for role in ("primary", "confirmation"):
+                rec = term.get(role)
+                if not rec:
+                    continue
+                for audit in rec.get("block_audit") or []:
+                    cases.append({"k": term["k"], "role": role, "wheel": rec["wheel"],
+                                  "M": rec["N"], "R": rec["residues_per_block"], "audit": audit})
+        json.dump({"source": "evidence/through400/runs.json (block_audit records of harness/run_k.py)",
+                   "recipe": "sha256 of the UTF-8 bytes of '\\n'.join(decimal(n) for n in sorted(survivors)), "
+                             "no trailing newline", "cases": cases},
+                  open(os.path.join(HERE, "replay_blocks.json"), "w"))
+        print("replay", len(cases), file=sys.stderr)
+
     if want("batch64"):
         ks, L = batch_instances(0, 64)
         insts = []

@@ -125,6 +125,43 @@ def test_k300_chunk_additivity_and_oracle(native):
     assert [int(x) for x in ctx.stage_counts()] == c_all
 
 
+def test_wide_inner_rings_vs_c_oracle(native):
+    """Recorded frontier wheels with 72..84-slot inner rings (three words: the four-word-row
+    instance, and the generic one inside a batch of mixed widths): 2^24 positions at an odd
+    offset of block 0, survivors and per-stage counts against the C oracle, F = 3..5."""
+    import es_gb300
+    import es_oracle as O
+    N = native
+    g = golden("replay_blocks.json")
+    picks = {(379, "primary"), (380, "confirmation")}
+    wheels = {(c["k"], c["role"]): c["wheel"] for c in g["cases"] if (c["k"], c["role"]) in picks}
+    for (k, role), wheel in sorted(wheels.items()):
+        plan = es_gb300.Plan(k, None, wheel)
+        r0 = plan.radix[0]
+        assert 64 < r0 <= 96
+        n = (1 << 24) // r0
+        ob = 987654321
+        ws, wc, _ = O.scan_c(plan, 0, o_range=(ob, ob + n))
+        for F in (3, 4, 5):
+            ctx = N.Context(plan, _tune(N, mask_filters=F, strip=3))
+            s, c = _scan(N, ctx, 0, ob, ob + n)
+            assert s == ws and c == wc, (k, role, F)
+            ctx.close()
+    # a batch mixing one- and three-word rings runs the generic instance
+    plans = [es_gb300.Plan(300), es_gb300.Plan(379, None, wheels[(379, "primary")])]
+    ctxs = [N.Context(p, _tune(N)) for p in plans]
+    items = [(i, i, 0, 1000, 1000 + (1 << 20) // p.radix[0]) for i, p in enumerate(plans)]
+    b = N.Batch(ctxs, items, _tune(N, mask_filters=4, strip=2))
+    b.run(use_graph=False)
+    b.sync()
+    surv = b.survivors()
+    for i, (p, it) in enumerate(zip(plans, items)):
+        ws, wc, _ = O.scan_c(p, 0, o_range=(it[3], it[4]))
+        assert sorted(int(r["idx"]) for r in surv if r["item"] == i) == ws, i
+        assert [int(x) for x in b.item_counts(i)] == wc, i
+    b.close()
+
+
 def test_batch64_prefixes(native):
     """64 seeded instances (k in 150..400) in one persistent launch: per-item golden counts."""
     import es_gb300

@@ -81,3 +81,24 @@ def test_learned_filter_order_is_a_permutation():
     assert Q.rest == order and Q.M == P.M
     with pytest.raises(AssertionError):
         es_plan.Plan(150, None, [[p, T] for p, T in P.wheel], filter_order=order[1:])
+
+
+def test_recorded_block_audits_rebuild():
+    """Every recorded frontier block (evidence/through400/runs.json audits): the wheel rebuilds the
+    recorded M and R, and the survivor hash recipe reproduces the recorded hash from the
+    recorded survivors; the whole-block GPU replays compare against exactly these records."""
+    import es_gb300
+    from conftest import golden
+    g = golden("replay_blocks.json")
+    assert len(g["cases"]) > 50
+    plans = {}
+    for c in g["cases"]:
+        key = (c["k"], c["role"])
+        if key not in plans:
+            plans[key] = es_gb300.Plan(c["k"], None, c["wheel"])
+        P = plans[key]
+        assert str(P.M) == c["M"] and P.R == c["R"], key
+        a = c["audit"]
+        if a.get("survivors_n") is not None:
+            assert es_gb300.survivor_hash(int(n) for n in a["survivors_n"]) == a["sha256_survivors"], key
+            assert len(a["survivors_n"]) == a["kernel_survivors"]
