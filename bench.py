@@ -45,11 +45,11 @@ TABLE_TRAFFIC_BYTES = 283648 + 256
 # / positions, the same ncu capture): with the measured SM clock it gives the kernel's issue rate
 # against the issue peak (4 schedulers x 1 warp instruction per clock per SM), the bound that an
 # integer kernel with no DRAM or tensor work actually meets.
-WARP_INST_PER_CANDIDATE = 184941830 / 2 ** 30
+WARP_INST_PER_CANDIDATE = 185446259 / 2 ** 30
 # Integer thread-instructions the scan kernel executes per candidate on this workload
 # (sm__sass_thread_inst_executed_op_integer_pred_on.sum / positions, an ncu capture of the same
 # 2^30-position case): the achieved integer-op rate against the measured int32 peak.
-INT_THREAD_OPS_PER_CANDIDATE = 3136909549 / 2 ** 30
+INT_THREAD_OPS_PER_CANDIDATE = 3138200109 / 2 ** 30
 METRIC = "Gcand/s on 1 GB300 (% int peak)"
 
 
