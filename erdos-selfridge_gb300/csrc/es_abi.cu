@@ -155,6 +155,8 @@ struct es_batch {
     unsigned long long* d_unit = nullptr;
     unsigned long long* d_found = nullptr;
     unsigned long long* d_min = nullptr;
+    unsigned long long* d_item_next = nullptr;   // per-item warp-unit counters (several plans)
+    uint32_t n_items = 0;
     EsLaunch L{};
     int grid = 0;
     uint32_t words = 0;    // inner-ring words shared by every plan, 0 when they differ
@@ -842,14 +844,17 @@ int es_batch_create(es_ctx* const* ctxs, uint32_t n_ctx, const es_batch_item* it
     if (ce == cudaSuccess) ce = cudaMalloc(&b->d_items, sizeof(EsItem) * n_items);
     if (ce == cudaSuccess) ce = cudaMalloc(&b->d_tconst, 4ull * std::max<size_t>(h_tc.size(), 4));
     if (ce == cudaSuccess) ce = cudaMalloc(&b->d_counts, 8ull * cwords);
-    // scalars: [0] survivor count, [1] unit counter, then group_found[G], group_min[4G]
-    if (ce == cudaSuccess) ce = cudaMalloc(&b->d_surv_n, 8ull * (2 + 5ull * b->n_groups));
+    // scalars: [0] survivor count, [1] unit counter, then group_found[G], group_min[4G],
+    // item_next[n_items]
+    if (ce == cudaSuccess) ce = cudaMalloc(&b->d_surv_n, 8ull * (2 + 5ull * b->n_groups + n_items));
     b->surv_cap = ctxs[0]->surv_cap;
     if (ce == cudaSuccess) ce = cudaMalloc(&b->d_surv, sizeof(es_survivor) * b->surv_cap);
     if (ce != cudaSuccess) { es_batch_destroy(b); return cuda_fail(ce, "batch setup"); }
     b->d_unit = b->d_surv_n + 1;
     b->d_found = b->d_surv_n + 2;
     b->d_min = b->d_surv_n + 2 + b->n_groups;
+    b->d_item_next = b->d_surv_n + 2 + 5ull * b->n_groups;
+    b->n_items = n_items;
     for (uint32_t i = 0; i < n_items; ++i) {
         EsItem& it = b->h_items[i];
         it.tconst = b->d_tconst + (uintptr_t)it.tconst;
@@ -872,6 +877,7 @@ int es_batch_create(es_ctx* const* ctxs, uint32_t n_ctx, const es_batch_item* it
     L.nf_max = nf_max;
     L.direct = n_ctx == 1 ? 1u : 0u;
     L.unit_counter = b->d_unit;
+    L.item_next = b->d_item_next;
     L.surv = b->d_surv;
     L.surv_n = b->d_surv_n;
     L.surv_cap = b->surv_cap;
@@ -892,6 +898,7 @@ int es_batch_create(es_ctx* const* ctxs, uint32_t n_ctx, const es_batch_item* it
 static int batch_enqueue(es_batch* b) {
     ES_CUDA(cudaMemsetAsync(b->d_surv_n, 0, 16, b->stream), "memset");
     ES_CUDA(cudaMemsetAsync(b->d_found, 0xff, 8ull * b->n_groups, b->stream), "memset");
+    ES_CUDA(cudaMemsetAsync(b->d_item_next, 0, 8ull * b->n_items, b->stream), "memset");
     if (b->counts_words)
         ES_CUDA(cudaMemsetAsync(b->d_counts, 0, 8ull * b->counts_words, b->stream), "memset");
     if (b->L.total_units) {

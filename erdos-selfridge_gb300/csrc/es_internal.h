@@ -96,7 +96,8 @@ struct EsLaunch {
     uint32_t nf_max;               // largest filter count among the launch's plans
     uint32_t direct;               // 1: every item uses one plan (no CTA barriers after staging)
     uint32_t pad2;
-    unsigned long long* unit_counter;
+    unsigned long long* unit_counter;     // single-plan launches: next warp-unit
+    unsigned long long* item_next;        // several plans: next warp-unit of each item
     struct es_survivor* surv;
     unsigned long long* surv_n;
     uint64_t surv_cap;

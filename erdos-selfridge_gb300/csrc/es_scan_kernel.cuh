@@ -684,11 +684,11 @@ __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, u
 }
 
 // Work distribution.  A warp-unit is 32 lanes x `strip` consecutive ring-1 cycles (or list
-// entries) of one item.  Direct mode (every item of the launch uses one plan): the CTA stages
-// the plan's tables once, then each warp claims warp-units from the global counter on its own --
-// no CTA barrier after staging.  Chunk mode (several plans): a CTA claims a chunk of
-// warp-units, restages when the plan changes, and its warps claim the chunk's units from a
-// shared counter; the only barriers are at chunk/item boundaries.
+// entries) of one item.  Single-plan launches: the CTA stages the plan's tables once, then each
+// warp claims warp-units from the global counter on its own -- no CTA barrier after staging.
+// Several plans: a CTA works on one item at a time, its warps claim the item's warp-units from
+// the item's own counter, and the CTA synchronises only when it moves to another item (and
+// restages when that item's plan differs).
 //
 // Template: F = filters evaluated in the inner-ring stage (upper bound, runtime Feff <= F),
 // LAYOUT = word-mask or scalar tables, COUNT = per-stage pass counts, WT = words per inner ring
@@ -698,9 +698,7 @@ template <int F, int LAYOUT, bool COUNT, int WT>
 __global__ void __launch_bounds__(ES_LB_THREADS, ES_LB_MINB) es_scan_kernel(const __grid_constant__ EsLaunch L) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ EsInst si;
-    __shared__ unsigned long long s_u0, s_u1, s_end, s_next;
     __shared__ uint32_t s_item;
-    __shared__ int s_skip;
 
     const uint32_t tid = threadIdx.x;
     const uint32_t lane = tid & 31u;
@@ -750,69 +748,74 @@ __global__ void __launch_bounds__(ES_LB_THREADS, ES_LB_MINB) es_scan_kernel(cons
         return;
     }
 
+    // ---- several plans: a CTA works on one item at a time and its warps claim that item's
+    // warp-units from the item's own counter (no CTA barrier per unit); the CTA synchronises
+    // only to move to another item, restaging the plan when it changes.  CTAs start spread over
+    // the unit space in proportion to the items' work.
     uint32_t cur_inst = 0xffffffffu;
-    for (;;) {
-        // ---- CTA claims a chunk of warp-units; the size shrinks as the work runs out ---------
-        if (tid == 0) {
-            const unsigned long long cur = *reinterpret_cast<volatile unsigned long long*>(L.unit_counter);
-            const unsigned long long rem = cur < total ? total - cur : 0ull;
-            unsigned long long ch = rem / (2ull * gridDim.x);
-            if (ch < 1ull) ch = 1ull;
-            if (ch > (unsigned long long)L.chunk_max) ch = L.chunk_max;
-            const unsigned long long u0 = atomicAdd(L.unit_counter, ch);
-            s_u0 = u0;
-            s_u1 = (u0 + ch < total) ? u0 + ch : total;
+    if (tid == 0) {
+        const unsigned long long u0 = (unsigned long long)blockIdx.x * total / gridDim.x;
+        uint32_t lo = 0, hi = L.n_items;
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (items[mid].unit_begin <= u0) lo = mid; else hi = mid;
         }
-        __syncthreads();
-        const unsigned long long u1 = s_u1;
-        unsigned long long u = s_u0;
-        if (u >= total) break;
-        while (u < u1) {
-            if (tid == 0) {
-                uint32_t lo = 0, hi = L.n_items;
-                while (hi - lo > 1) {
-                    const uint32_t mid = (lo + hi) >> 1;
-                    if (items[mid].unit_begin <= u) lo = mid; else hi = mid;
+        s_item = lo;
+    }
+    __syncthreads();
+    for (;;) {
+        const uint32_t item_id = s_item;
+        if (item_id >= L.n_items) break;
+        const EsItem& item = items[item_id];
+        if (item.inst_id != cur_inst) {
+            // restage: the header and the small tables of this item's plan
+            if (tid == 0) si = *item.inst;
+            __syncthreads();
+            copy_words(reinterpret_cast<uint32_t*>(smem), reinterpret_cast<const uint32_t*>(si.small),
+                       si.small_bytes >> 2);
+            __syncthreads();
+            cur_inst = item.inst_id;
+        }
+        for (;;) {
+            unsigned long long w = 0;
+            int stop = 0;
+            if (lane == 0) {
+                const unsigned long long c = atomicAdd(L.item_next + item_id, 1ull);
+                if (c >= item.n_units) {
+                    stop = 1;
+                } else if (L.group_found) {
+                    const unsigned long long fnd =
+                        *reinterpret_cast<volatile unsigned long long*>(L.group_found + item.group);
+                    if (item.t > fnd) stop = 1;
                 }
-                const EsItem& it = items[lo];
-                unsigned long long e = it.unit_begin + it.n_units;
-                if (e > u1) e = u1;
-                int skip = 0;
+                w = item.unit_begin + c;
+            }
+            stop = __shfl_sync(0xffffffffu, stop, 0);
+            w = __shfl_sync(0xffffffffu, w, 0);
+            if (stop) break;
+            scan_unit<F, LAYOUT, COUNT, WT>(L, si, smem, Q, wcnt, wcnt_saddr, lane, w, item, item_id);
+        }
+        __syncthreads();   // every warp is done with this item before its tables may be replaced
+        if (tid == 0) {
+            // the next item with unclaimed warp-units, after this one cyclically; each pass of
+            // the loop above claims at least one unit, so the counters only grow and this ends
+            uint32_t nxt = L.n_items;
+            for (uint32_t j = 1; j <= L.n_items; ++j) {
+                const uint32_t i = (item_id + j) % L.n_items;
+                const EsItem& it = items[i];
+                const unsigned long long c = *reinterpret_cast<volatile unsigned long long*>(L.item_next + i);
+                if (c >= it.n_units) continue;
                 if (L.group_found) {
                     const unsigned long long fnd =
                         *reinterpret_cast<volatile unsigned long long*>(L.group_found + it.group);
-                    if (it.t > fnd) skip = 1;
+                    if (it.t > fnd) continue;
                 }
-                s_item = lo;
-                s_end = e;
-                s_next = u;
-                s_skip = skip;
+                nxt = i;
+                break;
             }
-            __syncthreads();
-            const uint32_t item_id = s_item;
-            const unsigned long long end = s_end;
-            if (!s_skip) {
-                const EsItem& item = items[item_id];
-                if (item.inst_id != cur_inst) {
-                    // restage: the header, small tables and this plan's staged fast tables
-                    if (tid == 0) si = *item.inst;
-                    __syncthreads();
-                    copy_words(reinterpret_cast<uint32_t*>(smem), reinterpret_cast<const uint32_t*>(si.small),
-                               si.small_bytes >> 2);
-                    __syncthreads();
-                    cur_inst = item.inst_id;
-                }
-                for (;;) {
-                    unsigned long long w = 0;
-                    if (lane == 0) w = atomicAdd(&s_next, 1ull);
-                    w = __shfl_sync(0xffffffffu, w, 0);
-                    if (w >= end) break;
-                    scan_unit<F, LAYOUT, COUNT, WT>(L, si, smem, Q, wcnt, wcnt_saddr, lane, w, item, item_id);
-                }
-            }
-            __syncthreads();
-            u = end;
+            s_item = nxt;
         }
+        __syncthreads();
     }
 }
 
