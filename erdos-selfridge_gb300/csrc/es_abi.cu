@@ -157,10 +157,15 @@ struct es_batch {
     unsigned long long* d_min = nullptr;
     unsigned long long* d_item_next = nullptr;   // per-item warp-unit counters (several plans)
     uint32_t n_items = 0;
-    EsLaunch L{};
-    int grid = 0;
-    uint32_t words = 0;    // inner-ring words shared by every plan, 0 when they differ
-    uint32_t filters = 0;  // inner-ring stage filters of the launched kernel
+    EsItem* d_items_launch = nullptr;  // the items grouped by width class, as the launches see them
+    // One persistent launch per inner-ring width class (1, 2, 3-4 words, wider): each runs the
+    // kernel instance specialised for its width instead of one generic instance for all.
+    struct Sub {
+        EsLaunch L{};
+        int grid = 0;
+        uint32_t words = 0;
+    };
+    std::vector<Sub> subs;
     bool ran = false;
 };
 
@@ -617,8 +622,7 @@ static int ctx_launch(es_ctx* c, uint64_t ob, uint64_t oe, const uint64_t* d_lis
     it.inst_id = 0;
     const uint32_t F = stage_filters(tn.layout, tn.mask_filters, I.n_filters, I.F_built);
     const SmemPlan sp = plan_smem((uint32_t)I.small_bytes, I.n_filters, tn, 0);
-    it.n_sm = 0;
-    it.sm_fast_words = 0;
+    it.caller = 0;
     L.items = nullptr;
     L.n_items = 1;
     L.threads = tn.threads;
@@ -755,6 +759,7 @@ int es_batch_destroy(es_batch* b) {
     if (b->exec) cudaGraphExecDestroy(b->exec);
     if (b->graph) cudaGraphDestroy(b->graph);
     cudaFree(b->d_items);
+    cudaFree(b->d_items_launch);
     cudaFree(b->d_tconst);
     cudaFree(b->d_counts);
     cudaFree(b->d_surv);
@@ -778,25 +783,15 @@ int es_batch_create(es_ctx* const* ctxs, uint32_t n_ctx, const es_batch_item* it
     if (!b) return fail(ES_ERR_NOMEM, "host allocation");
     b->tune = tune;
     b->ctxs.assign(ctxs, ctxs + n_ctx);
-    // launch-wide smem plan: the largest small block / filter count, one fast-table budget
-    uint32_t small_max = 0, nf_max = 1, F = tune.mask_filters;
-    for (uint32_t i = 0; i < n_ctx; ++i) {
-        const es_ctx* c = ctxs[i];
-        if (!c) { es_batch_destroy(b); return fail(ES_ERR_ARG, "null context in batch"); }
-        small_max = std::max<uint32_t>(small_max, c->h_inst.small_bytes);
-        nf_max = std::max<uint32_t>(nf_max, c->h_inst.n_filters);
-        F = std::min(F, stage_filters(tune.layout, tune.mask_filters, c->h_inst.n_filters, c->h_inst.F_built));
-    }
-    b->filters = F;
-    const SmemPlan sp = plan_smem(small_max, nf_max, tune, 0);
+    for (uint32_t i = 0; i < n_ctx; ++i)
+        if (!ctxs[i]) { es_batch_destroy(b); return fail(ES_ERR_ARG, "null context in batch"); }
     const uint64_t per_unit = 32ull * tune.strip;
-    b->words = ctxs[0]->h_inst.W;
-    for (uint32_t i = 1; i < n_ctx; ++i)
-        if (ctxs[i]->h_inst.W != b->words) b->words = 0;
+    // width class of a plan: the kernel instance its inner ring uses
+    auto width_class = [](uint32_t W) -> uint32_t { return W <= 2 ? W : (W <= 4 ? 4u : 0u); };
     std::vector<uint32_t> h_tc;
     b->h_items.resize(n_items);
     b->count_off.resize(n_items);
-    uint64_t units = 0, cwords = 0;
+    uint64_t cwords = 0;
     uint32_t max_group = 0;
     for (uint32_t i = 0; i < n_items; ++i) {
         const es_batch_item& s = items[i];
@@ -817,13 +812,10 @@ int es_batch_create(es_ctx* const* ctxs, uint32_t n_ctx, const es_batch_item* it
         it.o_end = s.o_end;
         const uint64_t ncyc = s.o_end > s.o_begin ? cycles_of(I, s.o_begin, s.o_end, &it.c_begin) : 0;
         it.c_end = it.c_begin + ncyc;
-        it.unit_begin = units;
         it.n_units = (ncyc + per_unit - 1) / per_unit;
-        units += it.n_units;
         it.group = s.group;
         it.inst_id = s.ctx_index;
-        it.n_sm = 0;
-        it.sm_fast_words = 0;
+        it.caller = i;
         // per-block constants tconst[j] = (t mod q)(M mod q) mod q
         it.tconst = reinterpret_cast<const uint32_t*>((uintptr_t)h_tc.size());  // patched below
         for (uint32_t f = 0; f < I.n_filters; ++f) {
@@ -838,73 +830,115 @@ int es_batch_create(es_ctx* const* ctxs, uint32_t n_ctx, const es_batch_item* it
     }
     b->n_groups = max_group + 1;
     b->counts_words = cwords;
+    // launch order: items grouped by width class (stable), one launch per class
+    std::vector<uint32_t> order(n_items);
+    for (uint32_t i = 0; i < n_items; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) {
+        return width_class(ctxs[items[x].ctx_index]->h_inst.W) < width_class(ctxs[items[y].ctx_index]->h_inst.W);
+    });
+    const uint32_t kMaxSubs = 4;
     cudaError_t ce = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
     if (ce == cudaSuccess) ce = cudaEventCreate(&b->ev0);
     if (ce == cudaSuccess) ce = cudaEventCreate(&b->ev1);
     if (ce == cudaSuccess) ce = cudaMalloc(&b->d_items, sizeof(EsItem) * n_items);
+    if (ce == cudaSuccess) ce = cudaMalloc(&b->d_items_launch, sizeof(EsItem) * n_items);
     if (ce == cudaSuccess) ce = cudaMalloc(&b->d_tconst, 4ull * std::max<size_t>(h_tc.size(), 4));
     if (ce == cudaSuccess) ce = cudaMalloc(&b->d_counts, 8ull * cwords);
-    // scalars: [0] survivor count, [1] unit counter, then group_found[G], group_min[4G],
-    // item_next[n_items]
-    if (ce == cudaSuccess) ce = cudaMalloc(&b->d_surv_n, 8ull * (2 + 5ull * b->n_groups + n_items));
+    // scalars: [0] survivor count, [1..4] unit counters of the launches, then group_found[G],
+    // group_min[4G], item_next[n_items]
+    if (ce == cudaSuccess) ce = cudaMalloc(&b->d_surv_n, 8ull * (1 + kMaxSubs + 5ull * b->n_groups + n_items));
     b->surv_cap = ctxs[0]->surv_cap;
     if (ce == cudaSuccess) ce = cudaMalloc(&b->d_surv, sizeof(es_survivor) * b->surv_cap);
     if (ce != cudaSuccess) { es_batch_destroy(b); return cuda_fail(ce, "batch setup"); }
     b->d_unit = b->d_surv_n + 1;
-    b->d_found = b->d_surv_n + 2;
-    b->d_min = b->d_surv_n + 2 + b->n_groups;
-    b->d_item_next = b->d_surv_n + 2 + 5ull * b->n_groups;
+    b->d_found = b->d_surv_n + 1 + kMaxSubs;
+    b->d_min = b->d_found + b->n_groups;
+    b->d_item_next = b->d_min + 4ull * b->n_groups;
     b->n_items = n_items;
     for (uint32_t i = 0; i < n_items; ++i) {
         EsItem& it = b->h_items[i];
         it.tconst = b->d_tconst + (uintptr_t)it.tconst;
         it.counts = tune.count_stages ? b->d_counts + b->count_off[i] : nullptr;
     }
+    // the launches, one per width class, each over its own unit space
+    std::vector<EsItem> launch_items(n_items);
+    uint32_t pos = 0;
+    while (pos < n_items) {
+        const uint32_t cls = width_class(ctxs[items[order[pos]].ctx_index]->h_inst.W);
+        uint32_t end = pos;
+        uint32_t small_max = 0, nf_max = 1, F = tune.mask_filters, first_ctx = items[order[pos]].ctx_index;
+        bool one_ctx = true;
+        uint32_t words = ctxs[first_ctx]->h_inst.W;
+        uint64_t units = 0;
+        while (end < n_items && width_class(ctxs[items[order[end]].ctx_index]->h_inst.W) == cls) {
+            const uint32_t ci = items[order[end]].ctx_index;
+            const es_ctx* c = ctxs[ci];
+            small_max = std::max<uint32_t>(small_max, c->h_inst.small_bytes);
+            nf_max = std::max<uint32_t>(nf_max, c->h_inst.n_filters);
+            F = std::min(F, stage_filters(tune.layout, tune.mask_filters, c->h_inst.n_filters, c->h_inst.F_built));
+            if (ci != first_ctx) one_ctx = false;
+            if (c->h_inst.W != words) words = 0;   // the generic instance reads each plan's width
+            EsItem it = b->h_items[order[end]];
+            it.unit_begin = units;
+            units += it.n_units;
+            launch_items[end] = it;
+            ++end;
+        }
+        es_batch::Sub sub;
+        sub.words = cls == 0 ? 0u : (cls == 4 && words == 0 ? 4u : (words ? words : cls));
+        const SmemPlan sp = plan_smem(small_max, nf_max, tune, 0);
+        EsLaunch& L = sub.L;
+        memset(&L, 0, sizeof(L));
+        L.items = b->d_items_launch + pos;
+        L.n_items = end - pos;
+        L.threads = tune.threads;
+        L.strip = tune.strip;
+        L.mask_filters = F;
+        L.total_units = units;
+        L.chunk_max = 16u * (tune.threads / 32u);
+        L.nf_max = nf_max;
+        L.direct = one_ctx ? 1u : 0u;
+        L.unit_counter = b->d_unit + b->subs.size();
+        L.item_next = b->d_item_next + pos;
+        L.surv = b->d_surv;
+        L.surv_n = b->d_surv_n;
+        L.surv_cap = b->surv_cap;
+        L.group_found = b->d_found;
+        L.smem_bytes = sp.bytes;
+        L.tconst_off = sp.tconst_off;
+        L.fast_off = sp.fast_off;
+        L.cnt_off = sp.cnt_off;
+        L.queue_off = sp.queue_off;
+        if (int e = grid_for(tune.layout, tune.count_stages, sub.words, F, tune, sp.bytes,
+                             std::max<uint64_t>(units, 1), &sub.grid)) {
+            es_batch_destroy(b);
+            return e;
+        }
+        b->subs.push_back(sub);
+        pos = end;
+    }
     ce = cudaMemcpy(b->d_items, b->h_items.data(), sizeof(EsItem) * n_items, cudaMemcpyHostToDevice);
+    if (ce == cudaSuccess)
+        ce = cudaMemcpy(b->d_items_launch, launch_items.data(), sizeof(EsItem) * n_items, cudaMemcpyHostToDevice);
     if (ce == cudaSuccess && !h_tc.empty())
         ce = cudaMemcpy(b->d_tconst, h_tc.data(), 4ull * h_tc.size(), cudaMemcpyHostToDevice);
     if (ce != cudaSuccess) { es_batch_destroy(b); return cuda_fail(ce, "batch upload"); }
-
-    EsLaunch& L = b->L;
-    memset(&L, 0, sizeof(L));
-    L.items = b->d_items;
-    L.n_items = n_items;
-    L.threads = tune.threads;
-    L.strip = tune.strip;
-    L.mask_filters = F;
-    L.total_units = units;
-    L.chunk_max = 16u * (tune.threads / 32u);
-    L.nf_max = nf_max;
-    L.direct = n_ctx == 1 ? 1u : 0u;
-    L.unit_counter = b->d_unit;
-    L.item_next = b->d_item_next;
-    L.surv = b->d_surv;
-    L.surv_n = b->d_surv_n;
-    L.surv_cap = b->surv_cap;
-    L.group_found = b->d_found;
-    L.smem_bytes = sp.bytes;
-    L.tconst_off = sp.tconst_off;
-    L.fast_off = sp.fast_off;
-    L.cnt_off = sp.cnt_off;
-    L.queue_off = sp.queue_off;
-    if (int e = grid_for(tune.layout, tune.count_stages, b->words, F, tune, sp.bytes, std::max<uint64_t>(units, 1), &b->grid)) {
-        es_batch_destroy(b);
-        return e;
-    }
     *out = b;
     return ES_OK;
 }
 
 static int batch_enqueue(es_batch* b) {
-    ES_CUDA(cudaMemsetAsync(b->d_surv_n, 0, 16, b->stream), "memset");
+    ES_CUDA(cudaMemsetAsync(b->d_surv_n, 0, 8ull * 5, b->stream), "memset");   // count + unit counters
     ES_CUDA(cudaMemsetAsync(b->d_found, 0xff, 8ull * b->n_groups, b->stream), "memset");
     ES_CUDA(cudaMemsetAsync(b->d_item_next, 0, 8ull * b->n_items, b->stream), "memset");
     if (b->counts_words)
         ES_CUDA(cudaMemsetAsync(b->d_counts, 0, 8ull * b->counts_words, b->stream), "memset");
-    if (b->L.total_units) {
-        int e = es_launch_scan(b->L, (int)b->tune.layout, (int)b->tune.count_stages, b->words, b->grid, b->stream);
+    for (const es_batch::Sub& sub : b->subs) {
+        if (!sub.L.total_units) continue;
+        int e = es_launch_scan(sub.L, (int)b->tune.layout, (int)b->tune.count_stages, sub.words, sub.grid, b->stream);
         if (e) return cuda_fail((cudaError_t)e, "scan launch");
     }
+    // survivors carry the caller's item index: the min-reduction reads the items in that order
     int e = es_launch_min(b->d_surv, b->d_surv_n, b->surv_cap, b->d_items, b->n_groups, b->d_min, b->stream);
     if (e) return cuda_fail((cudaError_t)e, "min launch");
     return ES_OK;
@@ -1100,6 +1134,7 @@ extern "C" int es_search_blocks_static(const es_ctx* c, uint64_t t0, uint32_t n_
         it.c_end = cbeg + ncyc;
         it.unit_begin = nu * i;
         it.n_units = nu;
+        it.caller = i;
         for (uint32_t f = 0; f < nf; ++f) {
             const uint64_t q = c->q[f];
             g_static_tconst[(size_t)i * ES_MAX_FILTERS + f] = (uint32_t)((t % q) * (uint64_t)(c->M % q) % q);

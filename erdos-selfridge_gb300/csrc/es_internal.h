@@ -81,8 +81,8 @@ struct EsItem {
     uint64_t n_units;
     uint32_t group;
     uint32_t inst_id;        // distinct per plan context within a launch
-    uint32_t n_sm;           // fast tables of filters [0, n_sm) are staged in smem
-    uint32_t sm_fast_words;  // words of fast tables staged
+    uint32_t caller;         // the item's index in the caller's list (survivor records carry it)
+    uint32_t pad;
 };
 
 struct EsLaunch {

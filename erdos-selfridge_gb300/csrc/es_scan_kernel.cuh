@@ -391,7 +391,7 @@ __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, u
         C.group_found = L.group_found;
         C.surv_cap = L.surv_cap;
         C.wcnt_saddr = wcnt_saddr;
-        C.item_id = item_id;
+        C.item_id = item.caller;
         C.group = item.group;
         C.t_blk = item.t;
         C.Feff = Feff;
