@@ -115,8 +115,6 @@ struct es_ctx {
     size_t arena_bytes = 0;
     uint64_t table_bytes = 0;
     std::vector<uint32_t> q;
-    std::vector<uint32_t> fast_words_mask;  // prefix words of word-mask tables, F_built + 1
-    std::vector<uint32_t> fast_words_bits;  // prefix words of bit tables, n_filters + 1
     u128 M = 1;
     uint32_t tconst[ES_MAX_FILTERS] = {0};
     uint64_t t = 0;
@@ -171,33 +169,22 @@ struct es_batch {
 
 namespace {
 
-// Shared-memory plan of one launch: [small | fast tables | tconst | counters].
+// Shared-memory plan of one launch: [small tables | per-warp stage counters | per-warp slots].
 struct SmemPlan {
-    uint32_t fast_off, tconst_off, cnt_off, queue_off, bytes;
-    uint32_t fast_words_cap;
+    uint32_t cnt_off, queue_off, bytes;
 };
 
-// per-warp survivor queue (64 entries x 28 bytes), must match the kernel's EsQueue
+// per-warp slot: entry queue, lane records, tail context (the kernel's EsQueue)
 constexpr uint32_t kQueueBytes = ES_QUEUE_BYTES;
 
-SmemPlan plan_smem(uint32_t small_max, uint32_t nf_max, const es_tune& tune, uint32_t fast_need) {
+SmemPlan plan_smem(uint32_t small_max, uint32_t nf_max, const es_tune& tune) {
     SmemPlan p;
     const uint32_t warps = tune.threads / 32u;
     const uint32_t queues = kQueueBytes * warps;
     // per-warp stage counters exist only in counting launches; shared memory is kept small so
     // that the driver's carveout leaves the rest of the SM's 256 KB to L1 (the phase tables)
     const uint32_t counters = tune.count_stages ? (uint32_t)align_up(4ull * nf_max * warps, 16) : 0u;
-    const uint32_t fixed_tail = counters + queues;
-    uint32_t budget = tune.smem_kb * 1024u;
-    const uint32_t optin = (uint32_t)(g_dev.smem_optin - 1024);
-    if (budget > optin) budget = optin;
-    uint32_t avail = budget > small_max + fixed_tail ? budget - small_max - fixed_tail : 0u;
-    uint32_t fast_bytes = std::min<uint32_t>(avail, 4u * fast_need);
-    fast_bytes = (uint32_t)(fast_bytes / 16u * 16u);
-    p.fast_off = small_max;
-    p.fast_words_cap = fast_bytes / 4u;
-    p.tconst_off = p.fast_off + fast_bytes;
-    p.cnt_off = p.tconst_off;
+    p.cnt_off = small_max;
     p.queue_off = p.cnt_off + counters;
     p.bytes = p.queue_off + queues;
     return p;
@@ -342,7 +329,6 @@ int es_ctx_create(const es_plan_desc* d, const es_tune* tune_in, es_ctx** out) {
         fc[f].off = bit_off[f];
         fc[f].rcp = (uint64_t)(((u128)1 << 64) / q);
     }
-    c->fast_words_bits = bit_off;
     auto admissible = [&](uint32_t f, uint32_t r) -> uint32_t {
         return (d->allowed[bit_off[f] + (r >> 5)] >> (r & 31u)) & 1u;
     };
@@ -438,7 +424,6 @@ int es_ctx_create(const es_plan_desc* d, const es_tune* tune_in, es_ctx** out) {
             }
         }
     }
-    c->fast_words_mask.assign(mask_off.begin(), mask_off.begin() + FB + 1);
     // pair tables (inner rings of at most two words): phase row phi holds P_f[phi] and then the
     // row a wrap past M selects, P_f[(phi + corr_f) mod q_f], so one load serves both sides of
     // the carry split; filter f starts at word 2 * mask_off[f]
@@ -621,7 +606,7 @@ static int ctx_launch(es_ctx* c, uint64_t ob, uint64_t oe, const uint64_t* d_lis
     it.group = 0;
     it.inst_id = 0;
     const uint32_t F = stage_filters(tn.layout, tn.mask_filters, I.n_filters, I.F_built);
-    const SmemPlan sp = plan_smem((uint32_t)I.small_bytes, I.n_filters, tn, 0);
+    const SmemPlan sp = plan_smem((uint32_t)I.small_bytes, I.n_filters, tn);
     it.caller = 0;
     L.items = nullptr;
     L.n_items = 1;
@@ -629,7 +614,6 @@ static int ctx_launch(es_ctx* c, uint64_t ob, uint64_t oe, const uint64_t* d_lis
     L.strip = tn.strip;
     L.mask_filters = F;
     L.total_units = it.n_units;
-    L.chunk_max = 16u * (tn.threads / 32u);
     L.nf_max = std::max<uint32_t>(I.n_filters, 1);
     L.direct = 1;
     L.unit_counter = c->d_unit;
@@ -638,8 +622,6 @@ static int ctx_launch(es_ctx* c, uint64_t ob, uint64_t oe, const uint64_t* d_lis
     L.surv_cap = c->surv_cap;
     L.group_found = nullptr;
     L.smem_bytes = sp.bytes;
-    L.tconst_off = sp.tconst_off;
-    L.fast_off = sp.fast_off;
     L.cnt_off = sp.cnt_off;
     L.queue_off = sp.queue_off;
     memcpy(L.tconst0, c->tconst, 4ull * I.n_filters);
@@ -886,7 +868,7 @@ int es_batch_create(es_ctx* const* ctxs, uint32_t n_ctx, const es_batch_item* it
         }
         es_batch::Sub sub;
         sub.words = cls == 0 ? 0u : (cls == 4 && words == 0 ? 4u : (words ? words : cls));
-        const SmemPlan sp = plan_smem(small_max, nf_max, tune, 0);
+        const SmemPlan sp = plan_smem(small_max, nf_max, tune);
         EsLaunch& L = sub.L;
         memset(&L, 0, sizeof(L));
         L.items = b->d_items_launch + pos;
@@ -895,7 +877,6 @@ int es_batch_create(es_ctx* const* ctxs, uint32_t n_ctx, const es_batch_item* it
         L.strip = tune.strip;
         L.mask_filters = F;
         L.total_units = units;
-        L.chunk_max = 16u * (tune.threads / 32u);
         L.nf_max = nf_max;
         L.direct = one_ctx ? 1u : 0u;
         L.unit_counter = b->d_unit + b->subs.size();
@@ -905,8 +886,6 @@ int es_batch_create(es_ctx* const* ctxs, uint32_t n_ctx, const es_batch_item* it
         L.surv_cap = b->surv_cap;
         L.group_found = b->d_found;
         L.smem_bytes = sp.bytes;
-        L.tconst_off = sp.tconst_off;
-        L.fast_off = sp.fast_off;
         L.cnt_off = sp.cnt_off;
         L.queue_off = sp.queue_off;
         if (int e = grid_for(tune.layout, tune.count_stages, sub.words, F, tune, sp.bytes,
@@ -1116,7 +1095,7 @@ extern "C" int es_search_blocks_static(const es_ctx* c, uint64_t t0, uint32_t n_
     const es_tune& tn = c->tune;
     const uint32_t nf = I.n_filters;
     const uint32_t F = stage_filters(tn.layout, tn.mask_filters, nf, I.F_built);
-    const SmemPlan sp = plan_smem((uint32_t)I.small_bytes, nf, tn, 0);
+    const SmemPlan sp = plan_smem((uint32_t)I.small_bytes, nf, tn);
     const uint64_t per_unit = 32ull * tn.strip;
     uint64_t cbeg = 0;
     const uint64_t ncyc = cycles_of(I, 0, I.n_outer, &cbeg);
@@ -1156,7 +1135,6 @@ extern "C" int es_search_blocks_static(const es_ctx* c, uint64_t t0, uint32_t n_
     L.strip = tn.strip;
     L.mask_filters = F;
     L.total_units = nu * n_blocks;
-    L.chunk_max = 16u * (tn.threads / 32u);
     L.nf_max = std::max<uint32_t>(nf, 1);
     L.direct = 1;
     L.unit_counter = d_unit;
@@ -1165,8 +1143,6 @@ extern "C" int es_search_blocks_static(const es_ctx* c, uint64_t t0, uint32_t n_
     L.surv_cap = out_cap;
     L.group_found = d_found;
     L.smem_bytes = sp.bytes;
-    L.tconst_off = sp.tconst_off;
-    L.fast_off = sp.fast_off;
     L.cnt_off = sp.cnt_off;
     L.queue_off = sp.queue_off;
     if (L.total_units) {

@@ -92,10 +92,8 @@ struct EsLaunch {
     uint32_t strip;
     uint32_t mask_filters;   // F requested (template F is the rounded-up instance)
     uint64_t total_units;          // warp-units: 32 lanes x strip ring-1 cycles (or list entries)
-    uint32_t chunk_max;            // most warp-units a CTA claims at once
     uint32_t nf_max;               // largest filter count among the launch's plans
     uint32_t direct;               // 1: every item uses one plan (no CTA barriers after staging)
-    uint32_t pad2;
     unsigned long long* unit_counter;     // single-plan launches: next warp-unit
     unsigned long long* item_next;        // several plans: next warp-unit of each item
     struct es_survivor* surv;
@@ -103,8 +101,6 @@ struct EsLaunch {
     uint64_t surv_cap;
     unsigned long long* group_found;  // per group: least block with a good survivor
     uint32_t smem_bytes;              // dynamic shared memory of the launch
-    uint32_t tconst_off;              // unused (block constants are read from the item)
-    uint32_t fast_off;                // byte offset of the staged fast tables in smem
     uint32_t cnt_off;                 // byte offset of the per-warp tail-stage counters in smem
     uint32_t queue_off;               // byte offset of the per-warp survivor queues in smem
     // single-plan launches carry their one item and block constants by value

@@ -50,7 +50,7 @@ TUNABLES.update({
     "layout": "auto",        # "auto" (pair or word-mask by table bytes) | "wordmask" | "pair" | "scalar"
     "threads": 512,          # CTA size
     "strip": 2,              # ring-1 cycles per lane per warp-unit
-    "smem_kb": 0,            # shared-memory budget for staged word-mask tables (0: read via L1)
+    "smem_kb": 0,            # accepted, no effect (phase tables are read through L1)
     "ctas_per_sm": 4,
     "count_stages": 0,       # per-filter-stage pass counts (es_stage_counts needs 1)
     "search_batch_log2": 34, # positions per multi-block search launch

@@ -77,7 +77,8 @@ typedef struct es_tune {
     uint32_t mask_filters;  /* filters in the inner-ring stage, 1..ES_MAX_MASK_FILTERS */
     uint32_t threads;       /* CTA size, multiple of 32 in [64, 512] */
     uint32_t strip;         /* ring-1 cycles per thread per work unit (strip depth) */
-    uint32_t smem_kb;       /* shared-memory budget per CTA for staged tables */
+    uint32_t smem_kb;       /* accepted, no effect: the phase tables are read through L1, which
+                               measured faster than staging them in shared memory */
     uint32_t ctas_per_sm;   /* persistent grid = SM count * ctas_per_sm */
     uint32_t count_stages;  /* 1: accumulate per-filter-stage pass counts */
     uint32_t reserved;
