@@ -11,9 +11,10 @@
 // accumulated on request.  All arithmetic is exact integer arithmetic.
 //
 // How it is organised (GB300-first, not the reference's per-plan NVRTC source):
-//  * One persistent kernel per launch; warps claim work units from a global atomic counter --
-//    no spin waits anywhere.  Items are ordered by (group, block), and a group's later blocks
-//    are skipped once a good survivor is known (block-ordered search).
+//  * One persistent kernel per launch; warps claim work units from atomic counters (one for a
+//    single-plan launch, one per item when a launch holds several plans) -- no spin waits
+//    anywhere.  A group's later blocks are skipped once a good survivor is known (block-ordered
+//    search).
 //  * Two-level strip mining.  A lane owns `strip` consecutive ring-1 cycles (cycle index =
 //    oidx / r1).  Rings >= 2 give b2 = sum term_j mod M, decoded once per strip and then
 //    stepped with a 128-bit delta table when the ring-2 digit advances.  Ring 1 is swept in a
@@ -25,9 +26,9 @@
 //    identity, sieve/gpu_sieve_v9.py:9-18), reduced with unsigned min instead of branches.
 //  * Inner ring: its terms are sorted once on the host, so the wrap (s >= M) is a suffix of the
 //    sorted slots; its start (the carry split) comes from 32-bit keys through a 512-bucket
-//    table.  Word-mask layout: a filter costs two table loads per 32 candidates,
-//    P_f[phase][w]; scalar layout: one residue + bit test per live candidate.  A warp leaves
-//    the cascade early when a ballot shows no live candidate.
+//    table.  Word-mask layout: a filter costs two phase-table loads, P_f[phase] and the row a
+//    wrap selects, per word (or per 16-byte row of up to four words); pair layout: one load
+//    that holds both rows; scalar layout: one residue + bit test per live candidate.
 //  * Inner words that still hold candidates after the inner-ring stage are queued per warp as
 //    one 16-byte entry per lane; a flush takes 32 entries, one candidate per lane (full warps,
 //    not single lanes), runs the next filters from 32-bit term residues, and gives only the
