@@ -162,6 +162,29 @@ def test_wide_inner_rings_vs_c_oracle(native):
     b.close()
 
 
+def test_k390_two_wheel_batch_vs_c_oracle(native):
+    """The k = 390 configuration's launch shape: both recorded wheels (two inner words, pair
+    tables) as two plans of one persistent launch, with the learned-style deeper inner stage
+    too; 2^22 positions of each at an odd offset, against the C oracle."""
+    import es_gb300
+    import es_oracle as O
+    N = native
+    g = golden("scan_k390_sample.json")["wheels"]
+    plans = [es_gb300.Plan(390, None, g[r]["wheel"]) for r in ("primary", "confirmation")]
+    ctxs = [N.Context(p, _tune(N)) for p in plans]
+    items = [(i, i, 0, 424242 + 7 * i, 424242 + 7 * i + (1 << 22) // p.radix[0]) for i, p in enumerate(plans)]
+    want = [O.scan_c(p, 0, o_range=(it[3], it[4]))[:2] for p, it in zip(plans, items)]
+    for F, strip in ((4, 2), (5, 4)):
+        b = N.Batch(ctxs, items, _tune(N, layout=2, mask_filters=F, strip=strip))
+        b.run(use_graph=True)
+        b.sync()
+        surv = b.survivors()
+        for i, (ws, wc) in enumerate(want):
+            assert sorted(int(r["idx"]) for r in surv if r["item"] == i) == ws, (F, i)
+            assert [int(x) for x in b.item_counts(i)] == wc, (F, i)
+        b.close()
+
+
 def test_batch64_prefixes(native):
     """64 seeded instances (k in 150..400) in one persistent launch: per-item golden counts."""
     import es_gb300
