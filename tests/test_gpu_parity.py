@@ -6,7 +6,6 @@ survivor re-verification, layout/shape independence).  Bit-exact throughout: sur
 lists, per-filter-stage pass counts and the block-ordered minimum.
 """
 import hashlib
-import math
 
 import numpy as np
 import pytest
