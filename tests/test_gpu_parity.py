@@ -126,8 +126,8 @@ def test_k300_chunk_additivity_and_oracle(native):
 
 def test_wide_inner_rings_vs_c_oracle(native):
     """Recorded frontier wheels with 72..84-slot inner rings (three words: the four-word-row
-    instance, and the generic one inside a batch of mixed widths): 2^24 positions at an odd
-    offset of block 0, survivors and per-stage counts against the C oracle, F = 3..5."""
+    instance, alone and in a batch that mixes widths): 2^24 positions at an odd offset of block
+    0, survivors and per-stage counts against the C oracle, F = 3..5."""
     import es_gb300
     import es_oracle as O
     N = native
@@ -146,7 +146,7 @@ def test_wide_inner_rings_vs_c_oracle(native):
             s, c = _scan(N, ctx, 0, ob, ob + n)
             assert s == ws and c == wc, (k, role, F)
             ctx.close()
-    # a batch mixing one- and three-word rings runs the generic instance
+    # a batch mixing one- and three-word rings: one launch per width class, caller item order kept
     plans = [es_gb300.Plan(300), es_gb300.Plan(379, None, wheels[(379, "primary")])]
     ctxs = [N.Context(p, _tune(N)) for p in plans]
     items = [(i, i, 0, 1000, 1000 + (1 << 20) // p.radix[0]) for i, p in enumerate(plans)]
