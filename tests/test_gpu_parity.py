@@ -195,7 +195,8 @@ def test_batch64_prefixes(native):
         assert [[p, T] for p, T in plan.wheel] == inst["plan"]["wheel"]
         ctxs.append(N.Context(plan, _tune(N)))
         items.append((i, i, 0, 0, inst["prefix_outer"]))
-    # the plans differ in inner-ring width, so the pair layout runs the generic word-mask instance
+    # the plans differ in inner-ring width: one launch per width class; with layout 2 the one-
+    # and two-word classes use pair tables and the three-word class the 16-byte-row word masks
     for graph, layout in ((False, 0), (True, 0), (False, 2)):
         b = N.Batch(ctxs, items, _tune(N, layout=layout, mask_filters=6, strip=2))
         b.run(use_graph=graph)
