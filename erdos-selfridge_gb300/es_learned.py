@@ -291,18 +291,38 @@ def probe(item: dict, tune=None, log2_pos: int | None = None, reps: int = 3) -> 
         ctx.reset()
         ctx.launch(0, n_outer)
         counts = [int(x) for x in ctx.stage_counts()]
-        ctx.set_tune(N.make_tune(**dict(tune, count_stages=0)))
-        ctx.reset()
-        ctx.launch_timed(0, n_outer)
-        ms = []
-        for _ in range(reps):
+        t_run = N.make_tune(**dict(tune, count_stages=0))
+        ctx.set_tune(t_run)
+        n_pos = n_outer * r0
+        blocks = 1
+        if n_pos < (1 << log2_pos) and n_outer >= ctx.n_outer:
+            # the whole block is shorter than the probe: time consecutive blocks in one graph-
+            # replayed launch, the way the block-ordered search issues them, so that a short
+            # block's launch overhead is not taken for its scan rate
+            blocks = int(min(64, -(-(1 << log2_pos) // n_pos)))
+        if blocks > 1:
+            items = [(0, b, b, 0, n_outer) for b in range(blocks)]   # one group per block: none skipped
+            bt = N.Batch([ctx], items, t_run)
+            try:
+                bt.run(use_graph=True)
+                bt.sync()
+                ms = []
+                for _ in range(reps):
+                    bt.run(use_graph=True)
+                    ms.append(bt.sync())
+            finally:
+                bt.close()
+        else:
             ctx.reset()
-            ms.append(ctx.launch_timed(0, n_outer))
+            ctx.launch_timed(0, n_outer)
+            ms = []
+            for _ in range(reps):
+                ctx.reset()
+                ms.append(ctx.launch_timed(0, n_outer))
         m = statistics.median(ms)
     finally:
         ctx.close()
-    n_pos = n_outer * r0
-    return {"gcand": n_pos / m / 1e6, "ms": m, "positions": n_pos, "counts": counts}
+    return {"gcand": blocks * n_pos / m / 1e6, "ms": m, "positions": n_pos, "blocks": blocks, "counts": counts}
 
 
 class _PlanLike:
