@@ -12,7 +12,9 @@ the number of rings.  This module
    re-plans (harness/plan_sweep.py:52-58), each with several filter orders;
 2. probes each on the GPU: 2^28 positions of block 0 -> Gcand/s and per-filter pass fractions;
 3. trains a 3-layer FP32 MLP (64 hidden, ReLU) with this library's own CUDA kernels
-   (es_mlp_*) to predict log throughput and log expected positions to the first survivor;
+   (es_mlp_*) to predict log throughput and the log-error of the analytic estimate of expected
+   positions to the first survivor (the planner's expected-checks formula is a good start; the
+   network learns what it misses, which needs far less data than learning positions outright);
 4. chooses, per k, the plan with the least predicted time = positions / throughput, and compares
    it on held-out k with the analytic choice (least expected checks, reference filter order).
 
@@ -360,7 +362,11 @@ def collect(ks, procs: int | None = None, log=None, tune=None) -> list[dict]:
 
 # ------------------------------------------------------------------ model fit and choice
 class CostModel:
-    """MLP on standardised features/targets; predicts (log throughput, log positions)."""
+    """MLP on standardised features/targets.  Outputs: log throughput (Gcand/s) and the log-error
+    of the analytic expected-positions estimate, log(positions) - log(true_cost); a plan's
+    predicted log time is log(true_cost) + output[1] - output[0] (``log_time``)."""
+
+    TARGETS = "log_tp, log_pos - log(true_cost)"
 
     def __init__(self, seed: int = 0, hidden: int = 64):
         self.seed, self.hidden = seed, hidden
@@ -368,7 +374,7 @@ class CostModel:
 
     def fit(self, rows, epochs: int = 600, batch: int = 256, lr: float = 2e-3) -> float:
         X = np.array([r["features"] for r in rows], dtype=np.float64)
-        Y = np.array([[r["log_tp"], r["log_pos"]] for r in rows], dtype=np.float64)
+        Y = np.array([[r["log_tp"], r["log_pos"] - math.log(r["true_cost"])] for r in rows], dtype=np.float64)
         self.xm, self.xs = X.mean(0), X.std(0) + 1e-6
         self.ym, self.ys = Y.mean(0), Y.std(0) + 1e-6
         self.mlp = MLP(X.shape[1], 2, self.hidden, self.seed)
@@ -378,8 +384,14 @@ class CostModel:
         X = (np.asarray(feats, dtype=np.float64) - self.xm) / self.xs
         return self.mlp.forward(X).astype(np.float64) * self.ys + self.ym
 
+    def log_time(self, feats, true_costs) -> list[float]:
+        """Predicted log time-to-completion (up to a constant) of plans with these features and
+        analytic expected checks."""
+        pred = self.predict(feats)
+        return [math.log(tc) + p[1] - p[0] for tc, p in zip(true_costs, pred)]
+
     def save(self, path: str) -> None:
-        json.dump({"feature_dim": FEATURE_DIM, "hidden": self.hidden, "seed": self.seed,
+        json.dump({"feature_dim": FEATURE_DIM, "targets": self.TARGETS, "hidden": self.hidden, "seed": self.seed,
                    "xm": self.xm.tolist(), "xs": self.xs.tolist(), "ym": self.ym.tolist(),
                    "ys": self.ys.tolist(), "params": self.mlp.params().tolist()}, open(path, "w"))
 
@@ -387,6 +399,7 @@ class CostModel:
     def load(cls, path: str) -> "CostModel":
         d = json.load(open(path))
         assert d["feature_dim"] == FEATURE_DIM, "model was trained on another feature set"
+        assert d.get("targets") == cls.TARGETS, "model was trained on other targets"
         m = cls(d["seed"], d["hidden"])
         m.xm, m.xs = np.array(d["xm"]), np.array(d["xs"])
         m.ym, m.ys = np.array(d["ym"]), np.array(d["ys"])
@@ -412,9 +425,8 @@ def evaluate(rows, model: CostModel, test_ks) -> dict:
     mean_tp = math.exp(float(model.ym[0]))
     per_k, err_l, err_a, speed = {}, [], [], []
     for k, cand in sorted(by_k.items()):
-        pred = model.predict([c["features"] for c in cand])
         actual = [c["log_pos"] - c["log_tp"] for c in cand]            # ln(time) up to a constant
-        pred_l = [p[1] - p[0] for p in pred]
+        pred_l = model.log_time([c["features"] for c in cand], [c["true_cost"] for c in cand])
         pred_a = [math.log(c["true_cost"]) - math.log(mean_tp) for c in cand]
         for a, pl, pa in zip(actual, pred_l, pred_a):
             err_l.append(abs(pl - a))
@@ -460,7 +472,7 @@ def learned_order(model: CostModel, plan, seed: int = 0) -> tuple[str, list[int]
     rng = np.random.default_rng(seed)
     cands = [(n, o) for n, o in _orders(plan, rng, shuffles=0)]
     pred = model.predict([features(plan.with_order(o)) for _, o in cands])
-    best = min(range(len(cands)), key=lambda i: pred[i][1] - pred[i][0])
+    best = max(range(len(cands)), key=lambda i: pred[i][0])   # same wheel: same positions
     return cands[best]
 
 
