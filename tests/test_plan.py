@@ -102,3 +102,20 @@ def test_recorded_block_audits_rebuild():
         if a.get("survivors_n") is not None:
             assert es_gb300.survivor_hash(int(n) for n in a["survivors_n"]) == a["sha256_survivors"], key
             assert len(a["survivors_n"]) == a["kernel_survivors"]
+
+
+def test_engine_replay_audits_equal_the_records():
+    """The audit records this engine produced on GB300 for whole recorded blocks (committed after
+    the runs) equal the reference's recorded ones field by field, and their hashes follow from
+    their survivors."""
+    import es_gb300
+    from conftest import golden
+    rec = {(c["k"], c["role"], c["audit"]["t"]): c["audit"] for c in golden("replay_blocks.json")["cases"]}
+    ours = golden("replays_gb300.json")["cases"]
+    assert len(ours) >= 5
+    for c in ours:
+        a, r = c["audit"], rec[(c["k"], c["role"], c["t"])]
+        for f in ("t", "residues_enumerated", "kernel_survivors", "after_n_gt_k_plus_1",
+                  "passed_ref_is_good", "survivors_n", "sha256_survivors"):
+            assert a[f] == r[f], (c["k"], c["role"], c["t"], f)
+        assert es_gb300.survivor_hash(int(n) for n in a["survivors_n"]) == a["sha256_survivors"]
