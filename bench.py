@@ -56,7 +56,7 @@ METRIC = "Gcand/s on 1 GB300 (% int peak)"
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--tune", type=json.loads, default=None, help="engine tune override (JSON)")
@@ -79,7 +79,7 @@ class Clocks:
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.th = threading.Thread(target=self._read, daemon=True)
             self.th.start()
@@ -89,6 +89,12 @@ class Clocks:
     def _read(self):
         for line in self.proc.stdout:
             self.lines.append(line.strip())
+
+    def wait_first(self, timeout: float = 5.0) -> None:
+        """Block until the sampler has produced a line, so that the timed region is covered."""
+        t0 = time.time()
+        while self.proc is not None and not self.lines and time.time() - t0 < timeout:
+            time.sleep(0.01)
 
     def stop(self) -> dict:
         if self.proc is None:
@@ -253,9 +259,11 @@ def main():
     peak_ops, _ = N.int_peak()
     # timed region: K device steps, L2 flushed between them (outside the events)
     clk = Clocks(local)
+    clk.start()
+    clk.wait_first()
     barrier(pg)
     torch.cuda.synchronize()
-    clk.start()
+    clk.lines.clear()   # samples from the timed region only
     ms = []
     t_wall = time.perf_counter()
     for _ in range(args.steps):
