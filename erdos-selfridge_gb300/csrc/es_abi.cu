@@ -182,7 +182,7 @@ SmemPlan plan_smem(uint32_t small_max, uint32_t nf_max, const es_tune& tune) {
     const uint32_t warps = tune.threads / 32u;
     const uint32_t queues = kQueueBytes * warps;
     // per-warp stage counters exist only in counting launches; shared memory is kept small so
-    // that the driver's carveout leaves the rest of the SM's 256 KB to L1 (the phase tables)
+    // that the CUDA driver's carveout leaves the rest of the SM's 256 KB to L1 (the phase tables)
     const uint32_t counters = tune.count_stages ? (uint32_t)align_up(4ull * nf_max * warps, 16) : 0u;
     p.cnt_off = small_max;
     p.queue_off = p.cnt_off + counters;

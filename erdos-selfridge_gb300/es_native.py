@@ -177,7 +177,7 @@ class PlanArrays:
 
 
 # L1 bytes the phase tables can count on beside the scan's ~51 KB of shared memory (each SM has
-# 256 KB for L1 and shared memory together; the driver's carveout for the scan is 64 KB)
+# 256 KB for L1 and shared memory together; the CUDA driver's carveout for the scan is 64 KB)
 L1_TABLE_BUDGET = 180 * 1024
 
 
