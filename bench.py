@@ -157,19 +157,26 @@ def cpu_sample(plan):
     return np.unique(np.random.default_rng(0).integers(0, (1 << LOG2_POS) // r0, size=1 << 19, dtype=np.uint64))
 
 
-def cpu_baseline_py(plan, outer, steps: int = 1):
+def cpu_baseline_py(plan, outer, steps: int = 1, pool=None):
     """The reference CPU path (Plan.idx_to_n + Kummer filters in cascade order) over the sample,
-    fanned out over every host core; returns (Gcand/s, cores, seconds/step)."""
+    fanned out over every host core on a persistent process pool (started and warmed outside
+    the timing); returns (Gcand/s, cores, seconds per step)."""
     import es_oracle as O
-    cores = os.cpu_count() or 1
-    V = O.PlanView(plan)
+    own = pool is None
+    if own:
+        pool = O.ScanPool(plan)
+        pool.scan(0, outer[:4096])
     times = []
-    for _ in range(steps):
-        t0 = time.perf_counter()
-        O.scan_mp(V, 0, outer, procs=cores)
-        times.append(time.perf_counter() - t0)
+    try:
+        for _ in range(steps):
+            t0 = time.perf_counter()
+            pool.scan(0, outer)
+            times.append(time.perf_counter() - t0)
+    finally:
+        if own:
+            pool.close()
     dt = min(times)
-    return outer.size * V.r0 / dt / 1e9, cores, dt
+    return outer.size * pool.V.r0 / dt / 1e9, pool.procs, dt
 
 
 def cpu_baseline_c(plan, outer):
@@ -188,17 +195,22 @@ def run_reference(args, rank, world, pg):
         return
     import es_gb300
     plan = es_gb300.Plan(K_BENCH)
+    import es_oracle as O
     outer = cpu_sample(plan)
     if args.steps > 30:   # keep the whole run within a few minutes: a smaller sample per step
         outer = outer[: max(4096, outer.size * 30 // args.steps)]
-    for _ in range(max(0, min(args.warmup, 1))):
-        cpu_baseline_py(plan, outer[:20000])
-    vals = []
-    t_all = time.perf_counter()
-    for _ in range(args.steps):
-        v, cores, dt = cpu_baseline_py(plan, outer)
-        vals.append((v, dt))
-    wall = time.perf_counter() - t_all
+    pool = O.ScanPool(plan)
+    try:
+        for _ in range(max(1, min(args.warmup, 3))):
+            pool.scan(0, outer[:20000])
+        vals = []
+        t_all = time.perf_counter()
+        for _ in range(args.steps):
+            v, cores, dt = cpu_baseline_py(plan, outer, pool=pool)
+            vals.append((v, dt))
+        wall = time.perf_counter() - t_all
+    finally:
+        pool.close()
     v = statistics.median(x for x, _ in vals)
     ms = statistics.median(d for _, d in vals) * 1e3
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "Gcand/s", "n_gpus": 0,

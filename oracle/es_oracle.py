@@ -176,21 +176,38 @@ def _mp_job(args):
     return scan_py(_MP_VIEW, t, outer)
 
 
+class ScanPool:
+    """The Python reference path on a persistent pool of ``procs`` spawned processes, so that
+    repeated scans (timed baseline steps) do not pay for starting the processes each time."""
+
+    def __init__(self, plan, procs: int | None = None):
+        self.V = plan if isinstance(plan, PlanView) else PlanView(plan)
+        self.procs = procs or os.cpu_count() or 1
+        self.pool = mp.get_context("spawn").Pool(self.procs, initializer=_mp_init, initargs=(self.V,))
+
+    def scan(self, t: int, outer) -> tuple[list[int], list[int]]:
+        outer = [int(x) for x in outer]
+        step = max(1, -(-len(outer) // (4 * self.procs)))
+        parts = [(t, outer[i:i + step]) for i in range(0, len(outer), step)]
+        res = self.pool.map(_mp_job, parts)
+        surv, counts = [], [0] * len(self.V.rest)
+        for s, c in res:
+            surv.extend(s)
+            counts = [a + b for a, b in zip(counts, c)]
+        return sorted(surv), counts
+
+    def close(self) -> None:
+        self.pool.close()
+        self.pool.join()
+
+
 def scan_mp(plan, t: int, outer, procs: int | None = None) -> tuple[list[int], list[int]]:
     """The Python reference path fanned out over ``procs`` processes (spawn start method)."""
-    V = plan if isinstance(plan, PlanView) else PlanView(plan)
-    outer = [int(x) for x in outer]
-    procs = procs or os.cpu_count() or 1
-    step = max(1, -(-len(outer) // (4 * procs)))
-    parts = [(t, outer[i:i + step]) for i in range(0, len(outer), step)]
-    ctx = mp.get_context("spawn")
-    with ctx.Pool(procs, initializer=_mp_init, initargs=(V,)) as pool:
-        res = pool.map(_mp_job, parts)
-    surv, counts = [], [0] * len(V.rest)
-    for s, c in res:
-        surv.extend(s)
-        counts = [a + b for a, b in zip(counts, c)]
-    return sorted(surv), counts
+    sp = ScanPool(plan, procs)
+    try:
+        return sp.scan(t, outer)
+    finally:
+        sp.close()
 
 
 # ------------------------------------------------------------------ C restatement
