@@ -37,20 +37,25 @@ for _p in (PKG, ORACLE):
 
 K_BENCH = 300
 LOG2_POS = 34
-# DRAM bytes per scan launch of this workload (dram__bytes_read.sum + dram__bytes_write.sum, one
-# ncu capture on GB300 of the 2^30-position case): the scan reads only its plan tables, once, so
-# the figure does not grow with the range (algorithmic HBM bytes per candidate: zero).
-TABLE_TRAFFIC_BYTES = 283648 + 256
-# Warp instructions the scan kernel issues per candidate on this workload (smsp__inst_executed.sum
-# / positions, the same ncu capture): with the measured SM clock it gives the kernel's issue rate
-# against the issue peak (4 schedulers x 1 warp instruction per clock per SM), the bound that an
-# integer kernel with no DRAM or tensor work actually meets.
-WARP_INST_PER_CANDIDATE = 185446259 / 2 ** 30
-# Integer thread-instructions the scan kernel executes per candidate on this workload
-# (sm__sass_thread_inst_executed_op_integer_pred_on.sum / positions, an ncu capture of the same
-# 2^30-position case): the achieved integer-op rate against the measured int32 peak.
-INT_THREAD_OPS_PER_CANDIDATE = 3138200109 / 2 ** 30
+# Per-candidate counters of the scan kernel on this workload, from one ncu capture (the command
+# and the launch shape they were taken with are in the file).  They apply only to that shape:
+# with any other --tune the bench omits the counter-based figures.
+COUNTERS_PATH = os.path.join(PKG, "data", "scan_counters_k300.json")
 METRIC = "Gcand/s on 1 GB300 (% int peak)"
+
+
+def load_counters(tune: dict, log2_positions: int):
+    """The measured per-candidate counters when they were captured on this launch shape, else
+    (None, why).  They are per candidate, so any range of the same workload may use them."""
+    try:
+        with open(COUNTERS_PATH) as f:
+            d = json.load(f)
+    except (OSError, ValueError) as e:
+        return None, f"no counters file ({e})"
+    if d.get("k") != K_BENCH or d.get("tune") != tune:
+        return None, (f"counters were captured with tune {d.get('tune')} on k={d.get('k')}; this run uses "
+                      f"{tune}, so the counter-based figures are omitted")
+    return d, None
 
 
 def parse():
@@ -62,6 +67,7 @@ def parse():
     ap.add_argument("--tune", type=json.loads, default=None, help="engine tune override (JSON)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--log2-positions", type=int, default=LOG2_POS)
+    ap.add_argument("--no-k390", action="store_true", help="skip the k=390 learned-vs-analytic scan")
     return ap.parse_args()
 
 
@@ -268,7 +274,7 @@ def main():
     ctx.set_tune(sieve.tune)
     for _ in range(max(3, args.warmup)):
         dev_step()
-    peak_ops, _ = N.int_peak()
+    peak_ops, _ = N.int_peak(mixed=False)
     # timed region: K device steps, L2 flushed between them (outside the events)
     clk = Clocks(local)
     clk.start()
@@ -298,7 +304,7 @@ def main():
         sieve._launch(o_begin, n_outer)
         n = int(sieve.out_n.get()[0])
         s = sieve.out[:n].get() if n else []
-        return n, len(s)
+        return n, s
     for _ in range(2):
         e2e_step()
     barrier(pg)
@@ -307,33 +313,68 @@ def main():
         flush.zero_()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        n_e, _ = e2e_step()
+        n_e, e2e_surv = e2e_step()
         e2e_ms.append((time.perf_counter() - t0) * 1e3)
     e2e_step_ms = max_over_ranks(pg, statistics.mean(e2e_ms))
     e2e_val = world * n_pos / (e2e_step_ms * 1e-3) / 1e9
     nf = len(plan.rest)
 
-    # roofline: W(k) = 10 + 8 * fbar int32 ops per candidate
+    # survivors of the timed range (every step scans the same range): each is mapped to n and
+    # re-verified on the host by the exact Kummer test over every prime <= k; a survivor that
+    # fails it is a DISAGREEMENT and ends the run
+    from es_plan import kummer_ok, primes_upto
+    surv_idx = sorted(int(x) for x in ctx.survivors())
+    ps = primes_upto(K_BENCH)
+    surv_n = [plan.idx_to_n(i, 0) for i in surv_idx]
+    exact = [all(kummer_ok(n, K_BENCH, p) for p in ps) for n in surv_n]
+    if not all(exact):
+        raise SystemExit(f"DISAGREEMENT: kernel survivors that fail the exact test: "
+                         f"{[str(n) for n, ok in zip(surv_n, exact) if not ok][:8]}")
+    survivors = {"kernel": len(surv_idx), "exact_verified": sum(exact),
+                 "n_gt_k_plus_1": sum(1 for n in surv_n if n > K_BENCH + 1),
+                 "n": [str(n) for n in surv_n[:16]], "e2e_same": sorted(int(x) for x in e2e_surv) == surv_idx,
+                 "how": "idx -> n by Plan.idx_to_n; every prime p <= k checked by Kummer's digit test"}
+
+    # roofline.  Integer work per candidate is measured (ncu counters of this kernel on this
+    # workload and launch shape, data/scan_counters_k300.json) and multiplied by the measured
+    # rate; the ceiling is the integer peak measured in this run with ALU- and FMA-pipe
+    # instructions together (es_int_peak_mixed), the ALU pipe alone beside it.
+    peak_mixed, _ = N.int_peak(mixed=True)
+    tune_now = N.tune_dict(sieve.tune)
+    ctr, ctr_note = load_counters(tune_now, args.log2_positions)
+    per_gpu = value / world * 1e9                                  # candidates / s on one GPU
     total = n_pos
     evals = total + sum(counts[:-1]) if counts else total
     fbar = evals / total
     W = 10 + 8 * fbar
-    achieved = value / world * 1e9 * W / 1e12   # per GPU, against one GPU's peak
-    peak = peak_ops / 1e12
     sm_hz = (clocks.get("sm_mhz") or clocks.get("sm_max_mhz") or 0) * 1e6
-    issue_peak = dev["sm_count"] * 4 * sm_hz
-    issue_ach = value / world * 1e9 * WARP_INST_PER_CANDIDATE
-    issue = {"achieved": issue_ach / 1e12, "peak": issue_peak / 1e12 if issue_peak else None,
-             "unit": "T warp-inst/s", "frac": issue_ach / issue_peak if issue_peak else None,
-             "warp_inst_per_candidate": WARP_INST_PER_CANDIDATE,
-             "source": "instructions per candidate from an ncu capture of this kernel on the "
-                       "2^30-position case; issue peak = SMs x 4 schedulers x SM clock sampled here"}
-    int_ach = value / world * 1e9 * INT_THREAD_OPS_PER_CANDIDATE
-    int_pipe = {"achieved": int_ach / 1e12, "peak": peak, "unit": "T int-ops/s", "frac": int_ach / peak_ops,
-                "int_thread_ops_per_candidate": INT_THREAD_OPS_PER_CANDIDATE,
-                "source": "executed integer thread-instructions per candidate (ncu "
-                          "sm__sass_thread_inst_executed_op_integer_pred_on) x Gcand/s, against the "
-                          "es_int_peak measurement of this run"}
+    roof = {"bound": "int", "unit": "T int-ops/s", "peak": peak_mixed / 1e12,
+            "peak_source": "measured in this run: es_int_peak_mixed (LOP3 + IMAD chains, the ALU and "
+                           "FMA pipes together: the integer ceiling of a kernel that issues both)",
+            "alu_pipe_peak": peak_ops / 1e12,
+            "model_frac": per_gpu * W / peak_mixed,
+            "model": f"the reference's scalar-cascade estimate W = 10 + 8*fbar = {W:.2f} int32 ops per "
+                     f"candidate (fbar = {fbar:.4f} from this run's stage counts); the word-mask cascade "
+                     "tests 32 candidates per table load and needs far fewer, so this is not a fraction "
+                     "of anything the kernel executes"}
+    if ctr is not None:
+        pc = ctr["per_candidate"]
+        int_ach = per_gpu * pc["int_thread_inst"]
+        issue_ach = per_gpu * pc["warp_inst"]
+        issue_peak = dev["sm_count"] * 4 * sm_hz
+        roof.update({"achieved": int_ach / 1e12, "frac": int_ach / peak_mixed,
+                     "frac_of_alu_pipe_peak": int_ach / peak_ops,
+                     "traffic": ctr["dram_bytes_per_launch"],
+                     "issue": {"achieved": issue_ach / 1e12, "peak": issue_peak / 1e12 if issue_peak else None,
+                               "unit": "T warp-inst/s", "frac": issue_ach / issue_peak if issue_peak else None,
+                               "source": "warp instructions per candidate (ncu smsp__inst_executed) x Gcand/s "
+                                         "against SMs x 4 schedulers x the SM clock sampled here"},
+                     "counters": {"file": os.path.relpath(COUNTERS_PATH, ROOT), "command": ctr["command"],
+                                  "int_thread_inst_per_candidate": pc["int_thread_inst"],
+                                  "warp_inst_per_candidate": pc["warp_inst"]}})
+    else:
+        roof.update({"achieved": None, "frac": None, "traffic": None, "note": ctr_note})
+
     line = {
         "metric": METRIC, "value": value, "unit": "Gcand/s", "n_gpus": world, "steps": args.steps,
         "warmup": max(3, args.warmup), "ms_per_step": ms_step, "higher_is_better": True,
@@ -343,19 +384,13 @@ def main():
                                f"(rank+1)*2^{args.log2_positions}) per rank",
                    "k": K_BENCH, "positions_per_rank": n_pos, "parallelism": f"{world} shard(s) of the block",
                    "l2": "tables (~0.3 MB) are L2/smem resident by design; a 256 MiB write flushes L2 "
-                         "between timed steps", "tune": N.tune_dict(sieve.tune)},
+                         "between timed steps", "tune": tune_now},
         "e2e": {"value": e2e_val, "unit": "Gcand/s", "h2d_bytes_per_step": 4 * nf,
-                "d2h_bytes_per_step": 8 + 40 * n_e, "ms_per_step": e2e_step_ms},
+                "d2h_bytes_per_step": 24 + 40 * n_e, "ms_per_step": e2e_step_ms},
         "gpu_launches": args.steps,
-        "roofline": {"bound": "int32", "achieved": achieved, "peak": peak, "unit": "Tops/s",
-                     "frac": achieved / peak, "traffic": TABLE_TRAFFIC_BYTES,
-                     "model": f"W=10+8*fbar int32 ops/candidate, fbar={fbar:.4f} (this run's stage counts); "
-                              "the word-mask cascade tests 32 candidates per table load, so it exceeds "
-                              "this scalar-cascade model (frac > 1)",
-                     "peak_source": "measured: es_int_peak IADD3/LOP3 microbenchmark, this run",
-                     "issue": issue, "int_pipe": int_pipe},
+        "roofline": roof,
         "clocks": clocks,
-        "survivors_per_step": n_surv,
+        "survivors": survivors,
         "stage_counts_first8": counts[:8],
         "counted_pass_ms": ms_counted,
         "wall_s_timed_region": wall,
@@ -387,6 +422,27 @@ def main():
                                  "ms_per_step": l_ms, "time_ratio_reference_over_learned": ms_step / l_ms}
     except Exception as e:  # the learned model is optional for the headline
         line["learned_order"] = {"error": str(e)[:200]}
+    # the k = 390 fixed-scope confirmation scan (both recorded wheels, [0, 2^40) of block 0 each,
+    # one persistent launch replayed from a CUDA graph), driven by the learned planner's cascade
+    # orders and by the analytic (reference) orders, each arm autotuned on its own orders
+    if rank == 0 and not args.no_k390:
+        try:
+            import es_configs
+            import es_learned
+            r = es_configs.k390_learned(es_learned.MODEL_PATH, 40, reps=3, autotune=True)
+            line["learned_vs_analytic_k390"] = {
+                "workload": "k=390 primary and confirmation wheels, positions [0, 2^40) of block 0 each, "
+                            "one persistent launch (CUDA graph)",
+                "learned_orders": r["learned_orders"],
+                "device_ms": {"learned": r["learned_ms"], "analytic": r["analytic_ms"]},
+                "wall_ms": {"learned": r["learned"]["wall_ms"], "analytic": r["analytic"]["wall_ms"]},
+                "time_ratio_analytic_over_learned": {"device": r["wall_ratio_analytic_over_learned"],
+                                                     "wall": r["analytic"]["wall_ms"] / r["learned"]["wall_ms"]},
+                "Gcand_s": {"learned": r["learned_Gcand_s"], "analytic": r["analytic_Gcand_s"]},
+                "tunes": {"learned": r["learned_tune"], "analytic": r["analytic_tune"]},
+                "survivors_identical": r["survivors_identical"], "disagreements": len(r["disagreements"])}
+        except Exception as e:
+            line["learned_vs_analytic_k390"] = {"error": str(e)[:300]}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         outer = cpu_sample(plan)
         v_py, cores, dt_py = cpu_baseline_py(plan, outer)

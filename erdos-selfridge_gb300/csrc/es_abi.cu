@@ -243,6 +243,16 @@ int es_device_info(int* sm_count, int* cc_major, int* cc_minor, uint64_t* smem_o
     return ES_OK;
 }
 
+int es_device_name(char* out, uint32_t cap) {
+    if (!out || cap == 0) return fail(ES_ERR_ARG, "null or empty output buffer");
+    int dev = 0;
+    ES_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
+    cudaDeviceProp prop;
+    ES_CUDA(cudaGetDeviceProperties(&prop, dev), "cudaGetDeviceProperties");
+    snprintf(out, cap, "%s", prop.name);
+    return ES_OK;
+}
+
 int es_ctx_destroy(es_ctx* c) {
     if (!c) return ES_OK;
     if (c->stream) cudaStreamSynchronize(c->stream);
@@ -711,10 +721,13 @@ int es_stage_counts(es_ctx* c, uint64_t* counts, uint32_t n) {
 
 int es_min_survivor(es_ctx* c, int* found, uint64_t* t, uint64_t* s_lo, uint64_t* s_hi) {
     if (!c || !found) return fail(ES_ERR_ARG, "null argument");
-    int e = es_launch_min(c->d_surv, c->d_surv_n, c->surv_cap, nullptr, 1, c->d_min, c->stream);
+    int e = es_launch_min(c->d_surv, c->d_surv_n, c->surv_cap, nullptr, 1, nullptr, c->d_min, c->stream);
     if (e) return cuda_fail((cudaError_t)e, "min launch");
     ES_CUDA(cudaMemcpyAsync(c->h_pin, c->d_min, 32, cudaMemcpyDeviceToHost, c->stream), "copy");
     ES_CUDA(cudaStreamSynchronize(c->stream), "kernel execution");
+    if (c->h_pin[0] == 2)
+        return fail(ES_ERR_OVERFLOW, "survivor buffer overflow: the minimum over the stored records "
+                                     "is not reliable; raise the capacity or scan fewer positions");
     *found = (int)c->h_pin[0];
     if (t) *t = c->h_pin[1];
     if (s_lo) *s_lo = c->h_pin[2];
@@ -918,7 +931,8 @@ static int batch_enqueue(es_batch* b) {
         if (e) return cuda_fail((cudaError_t)e, "scan launch");
     }
     // survivors carry the caller's item index: the min-reduction reads the items in that order
-    int e = es_launch_min(b->d_surv, b->d_surv_n, b->surv_cap, b->d_items, b->n_groups, b->d_min, b->stream);
+    int e = es_launch_min(b->d_surv, b->d_surv_n, b->surv_cap, b->d_items, b->n_groups, b->d_found,
+                          b->d_min, b->stream);
     if (e) return cuda_fail((cudaError_t)e, "min launch");
     return ES_OK;
 }
@@ -969,6 +983,11 @@ int es_batch_group_min(es_batch* b, uint32_t group, int* found, uint64_t* t, uin
     if (t) *t = v[1];
     if (s_lo) *s_lo = v[2];
     if (s_hi) *s_hi = v[3];
+    if (v[0] == 2)   // records were dropped: the minimum over the stored ones is not reliable
+        return fail(ES_ERR_OVERFLOW, "survivor buffer overflow in the batch; the least block of this "
+                                     "group holding a good survivor is t = " +
+                                     (v[1] == ~0ull ? std::string("none") : std::to_string(v[1])) +
+                                     "; rescan the group's blocks one at a time");
     return ES_OK;
 }
 
@@ -996,7 +1015,7 @@ int es_batch_survivors(es_batch* b, es_survivor* out, uint64_t cap, uint64_t* n)
     return ES_OK;
 }
 
-int es_int_peak(double* ops_per_s, double* ms_out) {
+static int int_peak_probe(int mix, double* ops_per_s, double* ms_out) {
     if (int e = device_facts()) return e;
     unsigned long long* sink = nullptr;
     ES_CUDA(cudaMalloc(&sink, 8), "cudaMalloc");
@@ -1007,11 +1026,13 @@ int es_int_peak(double* ops_per_s, double* ms_out) {
     float best = 1e30f;
     for (int rep = 0; rep < 4; ++rep) {
         cudaEventRecord(a);
-        int e = es_launch_int_peak(sink, grid, threads, iters, nullptr);
+        int e = es_launch_int_peak(sink, grid, threads, iters, mix, nullptr);
         cudaEventRecord(z);
         cudaError_t ce = cudaEventSynchronize(z);
         if (e || ce != cudaSuccess) {
             cudaFree(sink);
+            cudaEventDestroy(a);
+            cudaEventDestroy(z);
             return cuda_fail(e ? (cudaError_t)e : ce, "int peak kernel");
         }
         float v = 0.f;
@@ -1026,6 +1047,10 @@ int es_int_peak(double* ops_per_s, double* ms_out) {
     if (ms_out) *ms_out = best;
     return ES_OK;
 }
+
+int es_int_peak(double* ops_per_s, double* ms_out) { return int_peak_probe(0, ops_per_s, ms_out); }
+
+int es_int_peak_mixed(double* ops_per_s, double* ms_out) { return int_peak_probe(1, ops_per_s, ms_out); }
 
 }  // extern "C"
 
@@ -1074,6 +1099,13 @@ extern "C" int es_search_blocks_static(const es_ctx* c, uint64_t t0, uint32_t n_
     if (t0 > UINT64_MAX - n_blocks) return fail(ES_ERR_RANGE, "block range overflows");
     const EsInst& I = c->h_inst;
     if (I.n_filters > ES_MAX_FILTERS) return fail(ES_ERR_RANGE, "too many filters");
+    cudaStream_t st = (cudaStream_t)stream;
+    // The descriptors below are copied from host staging arrays that the next call overwrites; a
+    // captured copy would read them only when the graph runs, so capture is refused.
+    cudaStreamCaptureStatus cap_status = cudaStreamCaptureStatusNone;
+    ES_CUDA(cudaStreamIsCapturing(st, &cap_status), "cudaStreamIsCapturing");
+    if (cap_status != cudaStreamCaptureStatusNone)
+        return fail(ES_ERR_STATE, "es_search_blocks_static cannot be called while its stream is capturing");
     int dev = 0;
     ES_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
     if (dev < 0 || dev >= kMaxDevices) return fail(ES_ERR_RANGE, "device index out of range");
@@ -1090,7 +1122,6 @@ extern "C" int es_search_blocks_static(const es_ctx* c, uint64_t t0, uint32_t n_
     unsigned long long* d_found = d_unit + 1;
     EsItem* d_items = reinterpret_cast<EsItem*>(base + kStaticItemsOff);
     uint32_t* d_tc = reinterpret_cast<uint32_t*>(base + kStaticTconstOff);
-    cudaStream_t st = (cudaStream_t)stream;
 
     const es_tune& tn = c->tune;
     const uint32_t nf = I.n_filters;
@@ -1151,7 +1182,7 @@ extern "C" int es_search_blocks_static(const es_ctx* c, uint64_t t0, uint32_t n_
         int e = es_launch_scan(L, (int)tn.layout, 0, I.W, grid, st);
         if (e) return cuda_fail((cudaError_t)e, "scan launch");
     }
-    int e = es_launch_min(d_out, d_count, out_cap, d_items, 1, d_min, st);
+    int e = es_launch_min(d_out, d_count, out_cap, d_items, 1, d_found, d_min, st);
     if (e) return cuda_fail((cudaError_t)e, "min launch");
     return ES_OK;
 }

@@ -121,8 +121,11 @@ int es_scan_prepare(int smem_optin_bytes);
 int es_scan_occupancy(int layout, int count, uint32_t words, uint32_t mask_filters, int threads,
                       int smem_bytes, int* ctas_per_sm);
 int es_launch_scan(const EsLaunch& L, int layout, int count, uint32_t words, int grid, void* stream);
-// group_min: [n_groups][4] = {found, t, s_lo, s_hi}; items == nullptr means one group (0)
+// group_min: [n_groups][4] = {found, t, s_lo, s_hi}; items == nullptr means one group (0).
+// found = 2 flags a survivor count above cap; t is then group_found[g] (or ~0 when null).
 int es_launch_min(const struct es_survivor* surv, const unsigned long long* surv_n,
                   uint64_t cap, const EsItem* items, uint32_t n_groups,
-                  unsigned long long* group_min, void* stream);
-int es_launch_int_peak(unsigned long long* sink, int grid, int threads, int iters, void* stream);
+                  const unsigned long long* group_found, unsigned long long* group_min,
+                  void* stream);
+// mix = 0: ALU-pipe probe (IADD3 + LOP3); mix = 1: ALU + FMA-pipe probe (LOP3 + IMAD)
+int es_launch_int_peak(unsigned long long* sink, int grid, int threads, int iters, int mix, void* stream);

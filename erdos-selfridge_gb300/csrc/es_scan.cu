@@ -11,13 +11,26 @@
 namespace {
 
 // Block-ordered minimum per search group: least (t, s) over good survivors.
-// out[g*4 + 0] = found, [1] = t, [2] = s_lo, [3] = s_hi.
+// out[g*4 + 0] = found, [1] = t, [2] = s_lo, [3] = s_hi.  When the survivor count exceeds the
+// buffer (records were dropped), the stored records may miss the least one: found = 2 then
+// flags the overflow, t is the least block holding a good survivor as the scan kernel recorded
+// it in group_found (exact; ~0 when there is none or group_found is null) and s = 0.
 __global__ void es_min_kernel(const es_survivor* __restrict__ surv,
                               const unsigned long long* __restrict__ surv_n, uint64_t cap,
-                              const EsItem* __restrict__ items, unsigned long long* out) {
+                              const EsItem* __restrict__ items,
+                              const unsigned long long* __restrict__ group_found,
+                              unsigned long long* out) {
     const uint32_t g = blockIdx.x;
     uint64_t n = *surv_n;
-    if (n > cap) n = cap;
+    if (n > cap) {
+        if (threadIdx.x == 0) {
+            out[4 * g + 0] = 2ull;
+            out[4 * g + 1] = group_found ? group_found[g] : ~0ull;
+            out[4 * g + 2] = 0ull;
+            out[4 * g + 3] = 0ull;
+        }
+        return;
+    }
     uint64_t bt = ~0ull, bhi = ~0ull, blo = ~0ull;
     for (uint64_t i = threadIdx.x; i < n; i += blockDim.x) {
         const es_survivor r = surv[i];
@@ -58,24 +71,43 @@ __global__ void es_min_kernel(const es_survivor* __restrict__ surv,
     }
 }
 
-// Integer-pipe throughput probe: 8 independent chains per thread of IADD3 / LOP3 pairs.
+// Integer throughput probes, 8 independent chains per thread, 16 steps per iteration.
+// MIX = false: one IADD3-class add and one LOP3 per chain and step, both on the ALU pipe (the
+//   ALU pipe's ceiling, 16 lanes per clock per scheduler).
+// MIX = true: one LOP3 (ALU pipe) and one IMAD (mad.lo.u32 with a run-time multiplier, FMA pipe)
+//   per chain and step: the two integer pipes together, up to the issue limit of one warp
+//   instruction per clock per scheduler -- the ceiling of an integer kernel that, like the scan,
+//   issues both.
+// Ops counted = 16 per step per thread (lanes x instructions) in both modes.
+template <bool MIX>
 __global__ void __launch_bounds__(256) es_int_peak_kernel(unsigned long long* sink, int iters,
                                                          uint32_t seed) {
     uint32_t a0 = seed ^ threadIdx.x, a1 = a0 * 3u + 1u, a2 = a0 * 5u + 7u, a3 = a0 * 7u + 3u;
     uint32_t a4 = a0 + 11u, a5 = a1 ^ 0x55u, a6 = a2 + 0x99u, a7 = a3 ^ 0x1234u;
     const uint32_t c1 = seed * 13u + 5u, c2 = seed * 29u + 17u;
+    const uint32_t m1 = (seed | 1u) * 0x9e3779b1u, m2 = (seed | 3u) * 0x85ebca6bu;   // run-time odd
     for (int i = 0; i < iters; ++i) {
 #pragma unroll
         for (int u = 0; u < 16; ++u) {
-            // one IADD3 and one LOP3 per chain per step (ops counted = 16 per step per thread)
-            a0 = a0 + a1 + c1;
-            a1 = a1 + a2 + c2;
-            a2 = a2 + a3 + c1;
-            a3 = a3 + a4 + c2;
-            a4 = a4 + a5 + c1;
-            a5 = a5 + a6 + c2;
-            a6 = a6 + a7 + c1;
-            a7 = a7 + a0 + c2;
+            if (MIX) {
+                asm volatile("mad.lo.u32 %0, %0, %1, %2;" : "+r"(a0) : "r"(m1), "r"(a1));
+                asm volatile("mad.lo.u32 %0, %0, %1, %2;" : "+r"(a1) : "r"(m2), "r"(a2));
+                asm volatile("mad.lo.u32 %0, %0, %1, %2;" : "+r"(a2) : "r"(m1), "r"(a3));
+                asm volatile("mad.lo.u32 %0, %0, %1, %2;" : "+r"(a3) : "r"(m2), "r"(a4));
+                asm volatile("mad.lo.u32 %0, %0, %1, %2;" : "+r"(a4) : "r"(m1), "r"(a5));
+                asm volatile("mad.lo.u32 %0, %0, %1, %2;" : "+r"(a5) : "r"(m2), "r"(a6));
+                asm volatile("mad.lo.u32 %0, %0, %1, %2;" : "+r"(a6) : "r"(m1), "r"(a7));
+                asm volatile("mad.lo.u32 %0, %0, %1, %2;" : "+r"(a7) : "r"(m2), "r"(a0));
+            } else {
+                a0 = a0 + a1 + c1;
+                a1 = a1 + a2 + c2;
+                a2 = a2 + a3 + c1;
+                a3 = a3 + a4 + c2;
+                a4 = a4 + a5 + c1;
+                a5 = a5 + a6 + c2;
+                a6 = a6 + a7 + c1;
+                a7 = a7 + a0 + c2;
+            }
             asm volatile("lop3.b32 %0, %0, %1, %2, 0x96;" : "+r"(a0) : "r"(a1), "r"(c1));
             asm volatile("lop3.b32 %0, %0, %1, %2, 0x96;" : "+r"(a1) : "r"(a2), "r"(c2));
             asm volatile("lop3.b32 %0, %0, %1, %2, 0x96;" : "+r"(a2) : "r"(a3), "r"(c1));
@@ -134,14 +166,18 @@ int es_launch_scan(const EsLaunch& L, int layout, int count, uint32_t words, int
 }
 
 int es_launch_min(const es_survivor* surv, const unsigned long long* surv_n, uint64_t cap,
-                  const EsItem* items, uint32_t n_groups, unsigned long long* group_min,
-                  void* stream) {
+                  const EsItem* items, uint32_t n_groups, const unsigned long long* group_found,
+                  unsigned long long* group_min, void* stream) {
     if (n_groups == 0) return 0;
-    es_min_kernel<<<n_groups, 256, 0, (cudaStream_t)stream>>>(surv, surv_n, cap, items, group_min);
+    es_min_kernel<<<n_groups, 256, 0, (cudaStream_t)stream>>>(surv, surv_n, cap, items, group_found,
+                                                              group_min);
     return (int)cudaGetLastError();
 }
 
-int es_launch_int_peak(unsigned long long* sink, int grid, int threads, int iters, void* stream) {
-    es_int_peak_kernel<<<grid, threads, 0, (cudaStream_t)stream>>>(sink, iters, 0x2545f491u);
+int es_launch_int_peak(unsigned long long* sink, int grid, int threads, int iters, int mix, void* stream) {
+    if (mix)
+        es_int_peak_kernel<true><<<grid, threads, 0, (cudaStream_t)stream>>>(sink, iters, 0x2545f491u);
+    else
+        es_int_peak_kernel<false><<<grid, threads, 0, (cudaStream_t)stream>>>(sink, iters, 0x2545f491u);
     return (int)cudaGetLastError();
 }

@@ -5,8 +5,9 @@ per lane per work unit, i.e. residues per thread per unit = strip * r1 * r0), th
 (word-mask vs scalar) and the number of filters evaluated in the inner-ring stage.  None of
 these changes which candidates pass; the tuner only times.  Search: coordinate descent from the
 default shape over one parameter at a time, each candidate timed with CUDA events on a probe
-range (median of a few launches).  Results are cached in a JSON file keyed by the plan's
-signature (k, wheel, filter order) so a plan is tuned once per machine.
+range (median of a few launches).  Results are cached in a JSON file keyed by the plan (k,
+wheel, filter order) and the engine (a hash of the library's bytes, the device's name and SM
+count), so a plan is tuned once per library build and GPU model.
 """
 from __future__ import annotations
 
@@ -27,8 +28,21 @@ DEFAULT = dict(layout=N.LAYOUT_WORDMASK, mask_filters=4, threads=512, strip=2, s
                ctas_per_sm=4, count_stages=0)
 
 
+def engine_signature() -> str:
+    """What a cached shape was measured on: the engine library's bytes and the device's name and
+    SM count.  A rebuilt kernel or another GPU model gets its own cache entries."""
+    h = hashlib.sha256()
+    with open(N.LIB_PATH, "rb") as f:
+        for chunk in iter(lambda: f.read(1 << 20), b""):
+            h.update(chunk)
+    info = N.device_info()
+    return f"{h.hexdigest()[:16]}|{info.get('name', '?')}|{info['sm_count']}"
+
+
 def plan_signature(plan) -> str:
-    key = json.dumps({"k": plan.k, "wheel": [[p, T] for p, T in plan.wheel], "rest": plan.rest})
+    """Cache key of a plan's tuned shape: the plan (k, wheel, cascade order) and the engine."""
+    key = json.dumps({"k": plan.k, "wheel": [[p, T] for p, T in plan.wheel], "rest": plan.rest,
+                      "engine": engine_signature()})
     return hashlib.sha256(key.encode()).hexdigest()[:16]
 
 

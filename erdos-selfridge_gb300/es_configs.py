@@ -130,7 +130,8 @@ def k390(log2_positions: int = 40, filter_orders: dict | None = None, tune: dict
         order = (filter_orders or {}).get(role)
         plans[role] = es_gb300.Plan(390, None, wheel, filter_order=order)
     F = es_autotune.DEFAULT["mask_filters"]
-    t = dict(es_autotune.DEFAULT, layout=N.layout_for_plan(plans["primary"], F), **(tune or {}))
+    t = dict(es_autotune.DEFAULT, layout=N.layout_for_plan(plans["primary"], F))
+    t.update(tune or {})
     ctxs = [N.Context(plans[r], N.make_tune(**t)) for r in ("primary", "confirmation")]
     if autotune:
         small = [(i, i, 0, 0, min(c.n_outer, -(-(1 << tune_log2) // c.r0))) for i, c in enumerate(ctxs)]
@@ -141,11 +142,14 @@ def k390(log2_positions: int = 40, filter_orders: dict | None = None, tune: dict
         n_outer = min(c.n_outer, -(-pos // c.r0))
         items.append((i, i, 0, 0, n_outer))
     b = N.Batch(ctxs, items, N.make_tune(**t))
-    b.run(use_graph=True)
-    ms = [b.sync()]
-    for _ in range(reps - 1):
+    b.run(use_graph=True)          # the first run captures and instantiates the graph
+    b.sync()
+    ms, wall = [], []
+    for _ in range(max(1, reps)):
+        t0 = time.perf_counter()
         b.run(use_graph=True)
-        ms.append(b.sync())
+        ms.append(b.sync())        # device time: CUDA events around the replayed graph
+        wall.append((time.perf_counter() - t0) * 1e3)   # host wall time of the same run
     surv = b.survivors()
     b.close()
     res = {}
@@ -174,8 +178,8 @@ def k390(log2_positions: int = 40, filter_orders: dict | None = None, tune: dict
     ms_med = statistics.median(ms)
     for c in ctxs:
         c.close()
-    return {"wheels": res, "ms": ms_med, "Gcand_s": total_pos / ms_med / 1e6, "tune": t,
-            "cross_checked": True, "disagreements": disagree}
+    return {"wheels": res, "ms": ms_med, "wall_ms": statistics.median(wall), "Gcand_s": total_pos / ms_med / 1e6,
+            "tune": t, "cross_checked": True, "disagreements": disagree}
 
 
 def k390_learned(model_path: str, log2_positions: int = 40, reps: int = 2, autotune: bool = True) -> dict:

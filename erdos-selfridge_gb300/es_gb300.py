@@ -25,6 +25,7 @@ import hashlib
 import json
 import math
 import os
+import re
 import signal
 import subprocess
 import sys
@@ -280,7 +281,16 @@ class GpuSieve:
                 surv = self.scan_block(t)
                 found_t = t
             else:
-                found = self._scan_blocks(t, nb)
+                try:
+                    found = self._scan_blocks(t, nb)
+                except N.EsError as e:
+                    if e.code != N.ES_ERR_OVERFLOW:
+                        raise
+                    # more survivors than one buffer holds: the stored records may miss the
+                    # least good one, so these blocks (and the rest of the search) run one block
+                    # at a time through scan_block, whose chunked fallback drains every launch
+                    cap = per = 1
+                    continue
                 if found is None:
                     self.residues_checked += nb * P.R
                     t += nb
@@ -327,55 +337,84 @@ def free_vram_mib() -> int | None:
         return None
 
 
+_KNOWN_LINE = re.compile(r"\s*(\d+)\s+(\d+)(?:\s|$)")
+
+
 def load_known(*paths: str) -> dict[int, tuple[int, str]]:
-    """k -> (g, source) from whitespace 'k g' files; earlier files win (sieve/gpu_sieve_v9.py:571-581)."""
-    known: dict[int, tuple[int, str]] = {}
-    for path in paths:
-        if not path or not os.path.exists(path):
+    """Known terms for the CLI's b-file check: k -> (g(k), file name), read from text files of
+    'k g' lines (other lines ignored).  A k listed in several files keeps the first file's value,
+    and missing or empty paths are skipped -- the contract of sieve/gpu_sieve_v9.py:571-581."""
+    terms: dict[int, tuple[int, str]] = {}
+    for path in filter(None, paths):
+        if not os.path.isfile(path):
             continue
-        for line in open(path):
-            parts = line.split()
-            if len(parts) >= 2 and parts[0].isdigit() and parts[1].isdigit():
-                known.setdefault(int(parts[0]), (int(parts[1]), os.path.basename(path)))
-    return known
+        label = os.path.basename(path)
+        with open(path) as fh:
+            for m in filter(None, map(_KNOWN_LINE.match, fh)):
+                k, g = int(m.group(1)), int(m.group(2))
+                if k not in terms:
+                    terms[k] = (g, label)
+    return terms
 
 
-def main():
-    """CLI/JSON contract of sieve/gpu_sieve_v9.py:584-618."""
-    ap = argparse.ArgumentParser(description="GB300 CRT-wheel search for g(k), partial-power wheel")
+# The engine CLI: the flags, exit code 124 on --timeout and the one JSON line per k that
+# harness/replay_release.py:21-27 and the operators' scripts rely on (sieve/gpu_sieve_v9.py:584-618).
+_CLI_FLAGS = (
+    ("--plan-only", dict(action="store_true", help="print each plan's summary and stop")),
+    ("--tune", dict(type=json.loads, default=None, help="JSON dict overriding TUNABLES")),
+    ("--wheel", dict(type=json.loads, default=None,
+                     help="explicit wheel: JSON list of [p,T] (or bare p = full power)")),
+    ("--max-blocks", dict(type=int, default=None, help="stop after this many blocks")),
+    ("--timeout", dict(type=float, default=None, help="seconds; process exits 124 on expiry")),
+    ("--min-free-mib", dict(type=int, default=2048, help="skip a k when the GPU has less free memory")),
+    ("--bfile", dict(default=os.path.join(HERE, "..", "data", "b003458.txt"), help="known terms (k g)")),
+    ("--known", dict(default=os.path.join(HERE, "..", "data", "known_extra.txt"),
+                     help="further known terms (k g), after the b-file")),
+)
+
+
+def _cli_parser() -> argparse.ArgumentParser:
+    ap = argparse.ArgumentParser(description="g(k) by the CRT-wheel sieve on one GB300")
     ap.add_argument("k", type=int, nargs="+")
-    ap.add_argument("--plan-only", action="store_true")
-    ap.add_argument("--tune", type=json.loads, default=None, help="JSON dict overriding TUNABLES")
-    ap.add_argument("--wheel", type=json.loads, default=None,
-                    help="explicit wheel: JSON list of [p,T] (or bare p = full power)")
-    ap.add_argument("--max-blocks", type=int, default=None)
-    ap.add_argument("--timeout", type=float, default=None, help="seconds; process exits 124 on expiry")
-    ap.add_argument("--min-free-mib", type=int, default=2048)
-    ap.add_argument("--bfile", default=os.path.join(HERE, "..", "data", "b003458.txt"))
-    ap.add_argument("--known", default=os.path.join(HERE, "..", "data", "known_extra.txt"))
-    a = ap.parse_args()
-    if a.timeout:
-        signal.signal(signal.SIGALRM, lambda *_: (print(json.dumps({"status": "TIMEOUT"}), flush=True), os._exit(124)))
-        signal.setitimer(signal.ITIMER_REAL, a.timeout)
-    known = load_known(a.bfile, a.known)
-    for k in a.k:
-        plan = Plan(k, a.tune, a.wheel)
-        if a.plan_only:
-            print(json.dumps(plan.summary()))
-            continue
-        free = free_vram_mib()
-        if free is not None and free < a.min_free_mib:
-            print(json.dumps({"k": k, "status": "SKIPPED_LOW_VRAM", "free_mib": free}))
-            continue
-        sieve = GpuSieve(plan)
-        res = sieve.search(a.max_blocks, log=lambda s: print(s, file=sys.stderr, flush=True))
-        if res.get("status") == "FOUND" and k in known:
-            g_known, src = known[k]
-            res["matches_bfile"] = (res["g"] == g_known)
-            res["bfile"] = g_known
-            res["known_source"] = src
-        res["plan"] = plan.summary()
-        print(json.dumps(res, default=str), flush=True)
+    for flag, kw in _CLI_FLAGS:
+        ap.add_argument(flag, **kw)
+    return ap
+
+
+def _exit_on_timeout(seconds: float) -> None:
+    """After `seconds` of wall time: one {"status": "TIMEOUT"} line, then exit status 124."""
+    def expire(_sig, _frame):
+        sys.stdout.write(json.dumps({"status": "TIMEOUT"}) + "\n")
+        sys.stdout.flush()
+        os._exit(124)
+    signal.signal(signal.SIGALRM, expire)
+    signal.setitimer(signal.ITIMER_REAL, seconds)
+
+
+def _cli_result(k: int, args, known: dict) -> dict:
+    """The JSON record of one k: the plan summary alone (--plan-only), a skip when the GPU lacks
+    memory, or the search result with the b-file comparison and the plan summary appended."""
+    plan = Plan(k, args.tune, args.wheel)
+    if args.plan_only:
+        return plan.summary()
+    free = free_vram_mib()
+    if free is not None and free < args.min_free_mib:
+        return {"k": k, "status": "SKIPPED_LOW_VRAM", "free_mib": free}
+    res = GpuSieve(plan).search(args.max_blocks, log=lambda msg: print(msg, file=sys.stderr, flush=True))
+    if res.get("status") == "FOUND" and k in known:
+        g_known, source = known[k]
+        res.update(matches_bfile=res["g"] == g_known, bfile=g_known, known_source=source)
+    res["plan"] = plan.summary()
+    return res
+
+
+def main(argv=None):
+    args = _cli_parser().parse_args(argv)
+    if args.timeout:
+        _exit_on_timeout(args.timeout)
+    known = load_known(args.bfile, args.known)
+    for k in args.k:
+        print(json.dumps(_cli_result(k, args, known), default=str), flush=True)
 
 
 if __name__ == "__main__":

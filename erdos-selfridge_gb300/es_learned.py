@@ -353,6 +353,7 @@ def collect(ks, procs: int | None = None, log=None, tune=None) -> list[dict]:
                    "log_tp": math.log(pr["gcand"]), "log_pos": math.log(epos),
                    "true_cost": rec["true_cost"], "M_bits": rec["M_bits"], "R": rec["R"],
                    "counts": pr["counts"][:8], "probe_positions": pr["positions"],
+                   "rates": [float(x) for x in rec["rates"]],
                    "wheel": rec["spec"]["wheel"], "order": rec["spec"]["order"]}
             rows.append(row)
             if log and len(rows) % 200 == 0:
@@ -415,8 +416,25 @@ def split_ks(ks, held_out: int = 40, seed: int = 0):
     return [k for k in ks if k not in test], test
 
 
-def evaluate(rows, model: CostModel, test_ks) -> dict:
-    """Held-out comparison of the learned and the analytic planner."""
+# The analytic veto: the learned planner departs from the analytic planner's choice only when the
+# network predicts at least this much less time for its own choice (log scale, 5 %); otherwise the
+# analytic choice stands.
+VETO_LOG_MARGIN = math.log(1.05)
+
+
+def _analytic_evals(rates) -> float:
+    """Expected filter evaluations per candidate of a cascade with these conditional pass rates
+    (the analytic per-candidate cost: W = 10 + 8 * evaluations int32 ops, sieve/gpu_sieve_v9.py:25)."""
+    total, alive = 0.0, 1.0
+    for r in rates:
+        total += alive
+        alive *= r
+    return total
+
+
+def evaluate(rows, model: CostModel, test_ks, margin: float = VETO_LOG_MARGIN) -> dict:
+    """Held-out comparison of the learned and the analytic planner, with an ablation of what the
+    network adds over fixed order families."""
     by_k = {}
     for r in rows:
         if r["k"] in test_ks:
@@ -434,6 +452,8 @@ def evaluate(rows, model: CostModel, test_ks) -> dict:
         ref = [i for i, c in enumerate(cand) if c["ref_order"]]
         ia = min(ref, key=lambda i: cand[i]["true_cost"])             # analytic planner's choice
         il = min(range(len(cand)), key=lambda i: pred_l[i])           # learned choice
+        if pred_l[il] > pred_l[ia] - margin:                          # analytic veto
+            il = ia
         ib = min(range(len(cand)), key=lambda i: actual[i])           # best measured
         s = math.exp(actual[ia] - actual[il])
         speed.append(s)
@@ -445,34 +465,66 @@ def evaluate(rows, model: CostModel, test_ks) -> dict:
                     "analytic_gcand": cand[ia]["gcand"], "learned_gcand": cand[il]["gcand"]}
     geo = math.exp(statistics.fmean(math.log(x) for x in speed)) if speed else None
     # fixed-scope scans (fixed positions, the default wheel): the learned order's measured
-    # throughput against the reference order's; positions are equal, so time ratio = rate ratio
-    fixed = []
+    # throughput against the reference order's; positions are equal, so time ratio = rate ratio.
+    # Ablation: every order family on its own (the same family for every k), the family the
+    # analytic model prefers (fewest expected filter evaluations per candidate), and the best
+    # family in hindsight, against the network's per-k choice.
+    fixed, family = [], {}
     for k, cand in sorted(by_k.items()):
         dw = [c for c in cand if c["wheel_name"] == "default"]
         ref = [c for c in dw if c["ref_order"]]
         if not dw or not ref:
             continue
         pred = model.predict([c["features"] for c in dw])
+        ir = dw.index(ref[0])
         il = max(range(len(dw)), key=lambda i: pred[i][0])
+        if pred[il][0] < pred[ir][0] + margin:                        # analytic veto
+            il = ir
         fixed.append(dw[il]["gcand"] / ref[0]["gcand"])
         per_k[k]["fixed_scope_learned_order"] = dw[il]["order_name"]
         per_k[k]["fixed_scope_time_ratio"] = fixed[-1]
+        for c in dw:
+            family.setdefault(c["order_name"], {})[k] = c["gcand"] / ref[0]["gcand"]
+        if "rates" in dw[0]:
+            ia = min(range(len(dw)), key=lambda i: _analytic_evals(dw[i]["rates"]))
+            family.setdefault("analytic-model-choice", {})[k] = dw[ia]["gcand"] / ref[0]["gcand"]
     geo_fixed = math.exp(statistics.fmean(math.log(x) for x in fixed)) if fixed else None
+    n_fixed = len(fixed)
+
+    def geo(v):
+        return math.exp(statistics.fmean(math.log(x) for x in v)) if v else None
+    families = {name: geo(list(v.values())) for name, v in family.items() if len(v) == n_fixed}
+    fixed_only = {n: g for n, g in families.items() if n != "analytic-model-choice"}
+    best_family = max(fixed_only, key=fixed_only.get) if fixed_only else None
     return {"held_out_k": sorted(by_k), "n_candidates": sum(len(v) for v in by_k.values()),
             "fixed_scope_geomean_time_ratio_reference_over_learned_order": geo_fixed,
+            "fixed_scope_ablation": {
+                "geomean_time_ratio_reference_over_family": families,
+                "best_fixed_family": best_family,
+                "network_over_best_fixed_family": (geo_fixed / fixed_only[best_family]
+                                                   if best_family and geo_fixed else None),
+                "network_over_analytic_model_choice": (geo_fixed / families["analytic-model-choice"]
+                                                       if geo_fixed and families.get("analytic-model-choice")
+                                                       else None)},
+            "veto_log_margin": margin,
             "mae_log_time_learned": statistics.fmean(err_l) if err_l else None,
             "mae_log_time_analytic": statistics.fmean(err_a) if err_a else None,
             "geomean_time_ratio_analytic_over_learned": geo,
             "min_time_ratio": min(speed) if speed else None, "per_k": per_k}
 
 
-def learned_order(model: CostModel, plan, seed: int = 0) -> tuple[str, list[int]]:
+def learned_order(model: CostModel, plan, seed: int = 0, margin: float = VETO_LOG_MARGIN) -> tuple[str, list[int]]:
     """Cascade order of one wheel with the least predicted time among the order families the
-    model was trained on (a fixed-scope scan has fixed positions, so this is the fastest order)."""
+    model was trained on (a fixed-scope scan has fixed positions, so this is the fastest order).
+    The analytic (reference) order stands unless the network predicts at least ``margin`` (log)
+    more throughput for its choice."""
     rng = np.random.default_rng(seed)
     cands = [(n, o) for n, o in _orders(plan, rng, shuffles=0)]
     pred = model.predict([features(plan.with_order(o)) for _, o in cands])
     best = max(range(len(cands)), key=lambda i: pred[i][0])   # same wheel: same positions
+    ref = next(i for i, (n, _) in enumerate(cands) if n == "reference")
+    if pred[best][0] < pred[ref][0] + margin:
+        best = ref
     return cands[best]
 
 

@@ -75,6 +75,7 @@ def lib() -> C.CDLL:
         "es_last_error": ([], C.c_char_p),
         "es_abi_version": ([], i32),
         "es_device_info": ([C.POINTER(i32), C.POINTER(i32), C.POINTER(i32), pu64], i32),
+        "es_device_name": ([C.c_char_p, u32], i32),
         "es_ctx_create": ([C.POINTER(PlanDesc), C.POINTER(Tune), C.POINTER(P)], i32),
         "es_ctx_destroy": ([P], i32),
         "es_ctx_set_tune": ([P, C.POINTER(Tune)], i32),
@@ -102,6 +103,7 @@ def lib() -> C.CDLL:
         "es_batch_survivors": ([P, C.POINTER(Survivor), u64, pu64], i32),
         "es_batch_destroy": ([P], i32),
         "es_int_peak": ([C.POINTER(C.c_double), C.POINTER(C.c_double)], i32),
+        "es_int_peak_mixed": ([C.POINTER(C.c_double), C.POINTER(C.c_double)], i32),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -378,14 +380,19 @@ class Batch:
         return out[:got.value]
 
 
-def int_peak() -> tuple[float, float]:
-    """(int32 ops/s, ms) of the integer-pipe microbenchmark on the current device."""
+def int_peak(mixed: bool = False) -> tuple[float, float]:
+    """(int32 ops/s, ms) of an integer microbenchmark on the current device: the ALU pipe alone
+    (IADD3 + LOP3), or with ``mixed`` the ALU and FMA pipes together (LOP3 + IMAD)."""
     ops, ms = C.c_double(), C.c_double()
-    check(lib().es_int_peak(C.byref(ops), C.byref(ms)))
+    fn = lib().es_int_peak_mixed if mixed else lib().es_int_peak
+    check(fn(C.byref(ops), C.byref(ms)))
     return ops.value, ms.value
 
 
 def device_info() -> dict:
     s, a, b, o = C.c_int(), C.c_int(), C.c_int(), C.c_uint64()
     check(lib().es_device_info(C.byref(s), C.byref(a), C.byref(b), C.byref(o)))
-    return {"sm_count": s.value, "cc": (a.value, b.value), "smem_optin": o.value}
+    name = C.create_string_buffer(256)
+    check(lib().es_device_name(name, 256))
+    return {"sm_count": s.value, "cc": (a.value, b.value), "smem_optin": o.value,
+            "name": name.value.decode(errors="replace")}

@@ -110,6 +110,8 @@ const char* es_last_error(void);
 int es_abi_version(void);
 /* Device facts for the tuner: SM count, compute capability, opt-in shared memory per CTA. */
 int es_device_info(int* sm_count, int* cc_major, int* cc_minor, uint64_t* smem_optin_bytes);
+/* The current device's name (NUL-terminated, truncated to cap bytes): part of the tuner's cache key. */
+int es_device_name(char* out, uint32_t cap);
 
 /* ---- context: one plan on the device ---------------------------------------------------- */
 /* Replaces GpuSieve.__init__ (sieve/gpu_sieve_v9.py:426-498): copies term tables, filter bit
@@ -151,7 +153,8 @@ int es_stage_counts(es_ctx* ctx, uint64_t* counts, uint32_t n_filters);
 int es_reset_counts(es_ctx* ctx);
 /* Block-ordered minimum over the survivors since the last reset: the least n = t*M + s with
  * n > k+1 (replaces the host sort + first good in GpuSieve.search, gpu_sieve_v9.py:551-563;
- * the host still re-verifies it). found = 0 when there is none. */
+ * the host still re-verifies it). found = 0 when there is none.  ES_ERR_OVERFLOW when the
+ * survivor count exceeded the capacity (dropped records could hold the minimum). */
 int es_min_survivor(es_ctx* ctx, int* found, uint64_t* t, uint64_t* s_lo, uint64_t* s_hi);
 /* Launch + CUDA-event time of the scan kernel alone (milliseconds), synchronising. */
 int es_launch_timed(es_ctx* ctx, uint64_t ostart, uint64_t ocount, float* ms);
@@ -164,6 +167,10 @@ int es_batch_create(es_ctx* const* ctxs, uint32_t n_ctx, const es_batch_item* it
 int es_batch_run(es_batch* b, int use_graph);
 /* Synchronises; ms = device time of the last run (CUDA events around the whole sequence). */
 int es_batch_sync(es_batch* b, float* ms);
+/* Least good survivor of one search group.  ES_ERR_OVERFLOW when the batch's survivor count
+ * exceeded its buffer: *found = 2 and *t = the least block of the group that holds a good
+ * survivor (exact, from the scan's own per-group record; UINT64_MAX when none), *s_lo = *s_hi = 0;
+ * rescan that group's blocks one at a time to get the survivor itself. */
 int es_batch_group_min(es_batch* b, uint32_t group, int* found, uint64_t* t, uint64_t* s_lo,
                        uint64_t* s_hi);
 int es_batch_item_counts(es_batch* b, uint32_t item, uint64_t* counts, uint32_t n_filters);
@@ -176,12 +183,17 @@ int es_batch_destroy(es_batch* b);
  * start-up): blocks t0 .. t0+n_blocks-1 of an existing context scanned as one block-ordered
  * search in one persistent launch on `stream`, allocating nothing.  The caller passes the outputs:
  * d_out (out_cap survivor records), d_count (1 word, zeroed by the call) and d_min (4 words:
- * found, t, s_lo, s_hi of the least n = t*M + s > k+1).  Scratch lives in a file-scope device
+ * found, t, s_lo, s_hi of the least n = t*M + s > k+1).  found = 2 means the survivor count
+ * (*d_count) exceeded out_cap and records were dropped: the minimum is then unknown, d_min[1]
+ * is the least block holding a good survivor (exact; UINT64_MAX when none) and the caller
+ * retries with fewer blocks or a larger buffer.  Scratch lives in a file-scope device
  * array sized for ES_STATIC_MAX_BLOCKS blocks (about 57 KB, held by every GPU that loads the
  * library until exit); larger n_blocks is rejected with ES_ERR_RANGE.  Stage counts are not
- * accumulated.  The first call on a device looks up the scratch array's device address: make
- * it before any stream capture.  Every call shares the one scratch array, so calls that
- * overlap on the GPU race.  Asynchronous: synchronise `stream` before reading the outputs. */
+ * accumulated.  The first call on a device looks up the scratch array's device address.  The
+ * call must not be made while `stream` is capturing (it returns ES_ERR_STATE): its small
+ * descriptor copies come from host staging arrays that the next call reuses.  Every call shares
+ * the one scratch array, so calls that overlap on the GPU race.  Asynchronous: synchronise
+ * `stream` before reading the outputs. */
 #define ES_STATIC_MAX_BLOCKS 64
 int es_search_blocks_static(const es_ctx* ctx, uint64_t t0, uint32_t n_blocks, es_survivor* d_out,
                             uint64_t out_cap, unsigned long long* d_count, unsigned long long* d_min,
@@ -204,9 +216,12 @@ int es_mlp_train(es_mlp* m, const float* X, const float* T, uint64_t n, uint32_t
                  uint32_t batch, float lr, uint64_t seed, float* final_loss);
 
 /* ---- measurement -------------------------------------------------------------------------- */
-/* Integer-pipe peak microbenchmark: int32 operations per second of a dependent-free mix of
- * IADD3 / LOP3 / IMAD-class instructions across the whole GPU (ops = lanes x instructions). */
+/* Integer peak microbenchmarks over the whole GPU (ops = lanes x instructions, dependent-free
+ * chains).  es_int_peak: IADD3 and LOP3 only, the ALU pipe's ceiling.  es_int_peak_mixed: LOP3
+ * paired with IMAD (mad.lo.u32, FMA pipe), the two integer pipes together -- the integer
+ * ceiling of a kernel such as the scan, which issues both (the roofline denominator). */
 int es_int_peak(double* ops_per_s, double* ms);
+int es_int_peak_mixed(double* ops_per_s, double* ms);
 
 #ifdef __cplusplus
 }

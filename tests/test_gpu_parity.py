@@ -307,3 +307,80 @@ def test_edge_ranges(native):
     assert [int(x) for x in ctx.stage_counts()] == wc
     with pytest.raises(N.EsError):
         ctx.launch(ctx.n_outer, 1)
+
+
+def test_k390_autotuned_config_vs_c_oracle(native):
+    """The k = 390 configuration as the measurement runs it: both recorded wheels in one
+    persistent launch, with the launch shape the batch autotuner picks for them, in the reference
+    (analytic) cascade orders and in the learned planner's orders; 2^26 positions of each wheel
+    at an odd offset, survivors and per-stage counts against the C oracle."""
+    import es_autotune
+    import es_configs
+    import es_gb300
+    import es_learned
+    import es_oracle as O
+    N = native
+    model = es_learned.CostModel.load(es_learned.MODEL_PATH)
+    for arm in ("analytic", "learned"):
+        plans = []
+        for wheel in es_configs.K390_WHEELS.values():
+            P = es_gb300.Plan(390, None, wheel)
+            if arm == "learned":
+                P = P.with_order(es_learned.learned_order(model, P)[1])
+            plans.append(P)
+        F = es_autotune.DEFAULT["mask_filters"]
+        start = dict(es_autotune.DEFAULT, layout=N.layout_for_plan(plans[0], F))
+        ctxs = [N.Context(p, N.make_tune(**start)) for p in plans]
+        probe = [(i, i, 0, 0, min(c.n_outer, (1 << 30) // c.r0)) for i, c in enumerate(ctxs)]
+        tune, _ = es_autotune.tune_batch(ctxs, probe, start=start)
+        assert all(tune[key] in vals for key, vals in es_autotune.SPACE.items()), tune
+        n = (1 << 26) // plans[0].radix[0]
+        items = [(i, i, 0, 777777 + 5 * i, 777777 + 5 * i + n) for i in range(len(plans))]
+        b = N.Batch(ctxs, items, N.make_tune(**dict(tune, count_stages=1)))
+        b.run(use_graph=True)
+        b.sync()
+        surv = b.survivors()
+        for i, (P, it) in enumerate(zip(plans, items)):
+            ws, wc, _ = O.scan_c(P, 0, o_range=(it[3], it[4]))
+            assert sorted(int(r["idx"]) for r in surv if r["item"] == i) == ws, (arm, i, tune)
+            assert [int(x) for x in b.item_counts(i)] == wc, (arm, i, tune)
+        b.close()
+        for c in ctxs:
+            c.close()
+
+
+def test_autotune_plan_shape_is_exact(native, tmp_path):
+    """es_autotune.tune_plan on a small plan: the shape it returns lies in its search space, is
+    cached (a second call returns it without timing), and the survivors and per-stage counts under
+    it equal the C oracle's."""
+    import es_autotune
+    import es_gb300
+    import es_oracle as O
+    N = native
+    plan = es_gb300.Plan(250)
+    cache = str(tmp_path / "tune.json")
+    space = {"strip": [1, 2, 4], "mask_filters": [3, 4, 5], "layout": [0, 2, 1], "threads": [256, 512]}
+    tune = es_autotune.tune_plan(plan, probe_log2=26, cache=cache, space=space)
+    assert all(tune[key] in vals for key, vals in es_autotune.SPACE.items()), tune
+    assert es_autotune.tune_plan(plan, probe_log2=26, cache=cache, space=space) == tune
+    ctx = N.Context(plan, N.make_tune(**dict(tune, count_stages=1)))
+    ob = 31337
+    n = (1 << 24) // plan.radix[0]
+    s, c = _scan(N, ctx, 0, ob, ob + n)
+    ws, wc, _ = O.scan_c(plan, 0, o_range=(ob, ob + n))
+    assert s == ws and c == wc, tune
+    ctx.close()
+
+
+def test_whole_recorded_block_replay(native):
+    """One whole recorded frontier block: k = 379, primary wheel, block 0 (7.17e14 positions, a
+    few minutes), every position through the drop-in scan_block; the reference driver's block
+    audit built from its survivors must equal the recorded one field by field (positions, kernel
+    survivors, survivors with n > k+1, survivors passing the exact test, sha256 of the sorted
+    survivors).  The record comes from the reference project's evidence/through400/runs.json."""
+    import es_configs
+    g = golden("replay_blocks.json")
+    case = next(c for c in g["cases"] if c["k"] == 379 and c["role"] == "primary" and c["audit"]["t"] == 0)
+    res = es_configs.replay([case])
+    assert res["all_match"], res["cases"][0]["fields"]
+    assert res["cases"][0]["audit"]["passed_ref_is_good"] == 1

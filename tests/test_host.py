@@ -1,67 +1,8 @@
 """CPU: host logic of the drop-in engine, with the device replaced by a fake backed by the C
 oracle (block loop, block-ordered search, DISAGREEMENT on a planted fault, overflow fallback)."""
-import numpy as np
 import pytest
 
-
-class FakeCtx:
-    """Stands in for es_native.Context; scans with the CPU oracle."""
-
-    def __init__(self, plan, capacity=1 << 20, plant=None):
-        import es_oracle as O
-        self.plan, self.capacity, self.plant = plan, capacity, plant
-        self.T = O.CTables(plan)
-        self.r0 = plan.radix[0] if plan.radix else 1
-        self.n_outer = plan.R // self.r0
-        self.n_filters = len(plan.rest)
-        self.t, self.surv = 0, []
-
-    def set_block(self, t, tconst=None):
-        self.t = int(t)
-
-    def reset(self):
-        self.surv = []
-
-    def launch(self, ostart, ocount):
-        import es_oracle as O
-        s, _, _ = O.scan_c(self.T, self.t, o_range=(ostart, ostart + ocount), threads=2)
-        self.surv.extend(s)
-        if self.plant is not None and ostart == 0:
-            self.surv.append(self.plant)
-
-    def count(self):
-        return len(self.surv)
-
-    def survivors(self):
-        if len(self.surv) > self.capacity:
-            raise RuntimeError("overflow")
-        return np.array(self.surv, dtype=np.uint64)
-
-
-class FakeBatch:
-    """Stands in for es_native.Batch: blocks of one group, least good (t, s)."""
-
-    def __init__(self, ctxs, items, tune=None):
-        self.ctx, self.items = ctxs[0], items
-
-    def run(self, use_graph=False):
-        from es_plan import is_admissible
-        self.best = None
-        for (_, _, t, ob, oe) in self.items:
-            self.ctx.set_block(t)
-            self.ctx.reset()
-            self.ctx.launch(ob, oe - ob)
-            P = self.ctx.plan
-            good = [n for n in (P.idx_to_n(int(i), t) for i in self.ctx.surv) if n > P.k + 1 and is_admissible(n, P.k)]
-            if good:
-                self.best = (t, min(good) - t * P.M)
-                return
-
-    def group_min(self, g):
-        return self.best
-
-    def close(self):
-        pass
+from fake_device import FakeBatch, FakeCtx
 
 
 def _sieve(monkeypatch, k, plant=None, cap=1 << 20, tun=None):
@@ -146,3 +87,23 @@ def test_layout_rule():
     assert N.layout_for(96, [1009, 1013], 2) == N.LAYOUT_WORDMASK
     assert es_gb300._tune_from(dict(es_gb300.TUNABLES), P300).layout == N.LAYOUT_WORDMASK
     assert es_gb300._tune_from(dict(es_gb300.TUNABLES, layout="scalar"), P300).layout == N.LAYOUT_SCALAR
+
+
+class _OverflowBatch(FakeBatch):
+    """A multi-block search launch whose survivor buffer overflowed (es_batch_group_min's
+    ES_ERR_OVERFLOW): the stored records may miss the least good survivor."""
+
+    def group_min(self, g):
+        import es_native as N
+        raise N.EsError(N.ES_ERR_OVERFLOW, "survivor buffer overflow in the batch")
+
+
+def test_batch_overflow_rescans_block_by_block(monkeypatch, bfile):
+    """An overflowing multi-block launch must not skip the block holding the answer: the search
+    rescans from the same block one block at a time (g(30) lies in block 9)."""
+    import es_gb300
+    sieve, fake = _sieve(monkeypatch, 30)
+    monkeypatch.setattr(es_gb300.N, "Batch", _OverflowBatch)
+    res = sieve.search(None)
+    assert res["status"] == "FOUND" and res["g"] == bfile[30] and res["block"] == 9
+    assert res["residues_checked"] == 10 * sieve.plan.R

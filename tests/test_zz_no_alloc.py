@@ -37,14 +37,18 @@ def _key(recs, t_max):
                   for r in recs if int(r["t"]) <= t_max)
 
 
-@pytest.mark.parametrize("k,t0,nb", [(60, 0, 16), (97, 0, 8), (70, 3, 20), (30, 0, 12)])
-def test_static_search_matches_batch(native, k, t0, nb):
+@pytest.mark.parametrize("k,t0,nb,count_stages", [(60, 0, 16, 0), (97, 0, 8, 0), (70, 3, 20, 0), (30, 0, 12, 0),
+                                                  (57, 0, 10, 1)])
+def test_static_search_matches_batch(native, bfile, k, t0, nb, count_stages):
+    """Two calls in a row against the allocating batch path, and the least n against g(k) of the
+    b-file (every block before g(k)'s holds no good survivor).  A context built for counting
+    launches works too: the static search never counts."""
     import torch
     import es_gb300
     N = native
     fn = _entry(N)
     plan = es_gb300.Plan(k)
-    ctx = N.Context(plan, N.make_tune(count_stages=0))
+    ctx = N.Context(plan, N.make_tune(count_stages=count_stages))
     # reference result: the allocating batch path, one group over the same blocks
     b = N.Batch([ctx], [(0, 0, t0 + i, 0, ctx.n_outer) for i in range(nb)], ctx.tune)
     b.run(use_graph=False)
@@ -71,6 +75,31 @@ def test_static_search_matches_batch(native, k, t0, nb):
         assert got_min == want_min
         assert got_min[0] * plan.M + got_min[1] > k + 1
         assert _key(_records(d_out, n), got_min[0]) == want
+        if t0 == 0:
+            assert got_min[0] * plan.M + got_min[1] == bfile[k]
+
+
+def test_static_search_overflow_is_flagged(native):
+    """More survivors than the caller's buffer holds: the count still says how many there were,
+    found = 2 flags the overflow, and d_min[1] is the least block holding a good survivor (the
+    block of g(k), which the allocating path reports too)."""
+    import torch
+    import es_gb300
+    N = native
+    fn = _entry(N)
+    k, nb = 30, 12                       # g(30) lies in block 9; blocks 0..9 hold 3 survivors
+    plan = es_gb300.Plan(k)
+    ctx = N.Context(plan, N.make_tune(count_stages=0))
+    cap = 1
+    d_out = torch.zeros(cap * N.SURVIVOR_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+    d_count = torch.zeros(1, dtype=torch.int64, device="cuda")
+    d_min = torch.zeros(4, dtype=torch.int64, device="cuda")
+    rc = fn(ctx.h, 0, nb, d_out.data_ptr(), cap, d_count.data_ptr(), d_min.data_ptr(), None)
+    assert rc == 0, N.lib().es_last_error().decode()
+    torch.cuda.synchronize()
+    assert int(d_count.item()) > cap
+    mn = [int(x) & ((1 << 64) - 1) for x in d_min.cpu().tolist()]
+    assert mn[0] == 2 and mn[1] == 9 and mn[2] == 0 and mn[3] == 0
 
 
 def test_static_search_rejects_oversize(native):
