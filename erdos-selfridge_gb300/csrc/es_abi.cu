@@ -77,8 +77,9 @@ int device_facts() {
 size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 int check_tune(const es_tune& t) {
-    if (t.layout != ES_LAYOUT_WORDMASK && t.layout != ES_LAYOUT_SCALAR && t.layout != ES_LAYOUT_PAIR)
-        return fail(ES_ERR_ARG, "tune.layout must be 0 (word-mask), 1 (scalar) or 2 (pair)");
+    if (t.layout != ES_LAYOUT_WORDMASK && t.layout != ES_LAYOUT_SCALAR && t.layout != ES_LAYOUT_PAIR &&
+        t.layout != ES_LAYOUT_SMEM)
+        return fail(ES_ERR_ARG, "tune.layout must be 0 (word-mask), 1 (scalar), 2 (pair) or 3 (shared-memory tables)");
     if (t.mask_filters < 1 || t.mask_filters > ES_MAX_MASK_FILTERS)
         return fail(ES_ERR_ARG, "tune.mask_filters must be in 1..8");
     if (t.threads < 64 || t.threads > 1024 || t.threads % 32)
@@ -162,6 +163,7 @@ struct es_batch {
         EsLaunch L{};
         int grid = 0;
         uint32_t words = 0;
+        uint32_t layout = 0;   // the layout this launch runs (launch_layout)
     };
     std::vector<Sub> subs;
     bool ran = false;
@@ -169,25 +171,40 @@ struct es_batch {
 
 namespace {
 
-// Shared-memory plan of one launch: [small tables | per-warp stage counters | per-warp slots].
+// Shared-memory plan of one launch:
+// [small tables | staged phase tables (ES_LAYOUT_SMEM) | per-warp stage counters | per-warp slots].
 struct SmemPlan {
-    uint32_t cnt_off, queue_off, bytes;
+    uint32_t stage_off, cnt_off, queue_off, bytes;
 };
 
 // per-warp slot: entry queue, lane records, tail context (the kernel's EsQueue)
 constexpr uint32_t kQueueBytes = ES_QUEUE_BYTES;
 
-SmemPlan plan_smem(uint32_t small_max, uint32_t nf_max, const es_tune& tune) {
+SmemPlan plan_smem(uint32_t small_max, uint32_t nf_max, const es_tune& tune, uint32_t stage_words = 0) {
     SmemPlan p;
     const uint32_t warps = tune.threads / 32u;
     const uint32_t queues = kQueueBytes * warps;
     // per-warp stage counters exist only in counting launches; shared memory is kept small so
-    // that the CUDA driver's carveout leaves the rest of the SM's 256 KB to L1 (the phase tables)
+    // that the CUDA driver's carveout leaves the rest of the SM's 256 KB to L1 (the phase tables),
+    // unless the launch stages those tables in shared memory itself
     const uint32_t counters = tune.count_stages ? (uint32_t)align_up(4ull * nf_max * warps, 16) : 0u;
-    p.cnt_off = small_max;
+    p.stage_off = small_max;
+    p.cnt_off = p.stage_off + (uint32_t)align_up(4ull * stage_words, 16);
     p.queue_off = p.cnt_off + counters;
     p.bytes = p.queue_off + queues;
     return p;
+}
+
+// The layout a launch actually runs: ES_LAYOUT_SMEM only for inner rings of one or two words
+// whose stage_words of inner-stage tables fit the opt-in shared memory beside the rest of the
+// launch's shared memory; otherwise the word-mask layout, which reads the same tables through L1.
+// Neither choice changes which candidates pass.
+uint32_t launch_layout(uint32_t layout, uint32_t words, uint32_t small_max, uint32_t nf_max,
+                       const es_tune& tune, uint32_t stage_words) {
+    if (layout != ES_LAYOUT_SMEM) return layout;
+    if (words != 1 && words != 2) return ES_LAYOUT_WORDMASK;
+    const SmemPlan p = plan_smem(small_max, nf_max, tune, stage_words);
+    return p.bytes <= (uint32_t)g_dev.smem_optin - 1024u ? ES_LAYOUT_SMEM : ES_LAYOUT_WORDMASK;
 }
 
 // Filters of the inner-ring stage actually compiled into the launched kernel: word-mask kernels
@@ -220,6 +237,8 @@ uint64_t cycles_of(const EsInst& I, uint64_t ob, uint64_t oe, uint64_t* cb) {
 }
 
 }  // namespace
+
+void es_set_last_error(const char* msg) { g_err = msg ? msg : ""; }
 
 // ------------------------------------------------------------------------------------------
 extern "C" {
@@ -616,7 +635,9 @@ static int ctx_launch(es_ctx* c, uint64_t ob, uint64_t oe, const uint64_t* d_lis
     it.group = 0;
     it.inst_id = 0;
     const uint32_t F = stage_filters(tn.layout, tn.mask_filters, I.n_filters, I.F_built);
-    const SmemPlan sp = plan_smem((uint32_t)I.small_bytes, I.n_filters, tn);
+    const uint32_t layout = launch_layout(tn.layout, I.W, I.small_bytes, I.n_filters, tn, I.mask_off[F]);
+    const SmemPlan sp = plan_smem((uint32_t)I.small_bytes, I.n_filters, tn,
+                                  layout == ES_LAYOUT_SMEM ? I.mask_off[F] : 0u);
     it.caller = 0;
     L.items = nullptr;
     L.n_items = 1;
@@ -634,12 +655,13 @@ static int ctx_launch(es_ctx* c, uint64_t ob, uint64_t oe, const uint64_t* d_lis
     L.smem_bytes = sp.bytes;
     L.cnt_off = sp.cnt_off;
     L.queue_off = sp.queue_off;
+    L.stage_off = sp.stage_off;
     memcpy(L.tconst0, c->tconst, 4ull * I.n_filters);
     if (it.n_units == 0) return ES_OK;
     int grid = 0;
-    if (int e = grid_for(tn.layout, tn.count_stages, I.W, F, tn, sp.bytes, it.n_units, &grid)) return e;
+    if (int e = grid_for(layout, tn.count_stages, I.W, F, tn, sp.bytes, it.n_units, &grid)) return e;
     ES_CUDA(cudaMemsetAsync(c->d_unit, 0, 8, c->stream), "memset");
-    int e = es_launch_scan(L, (int)tn.layout, (int)tn.count_stages, I.W, grid, c->stream);
+    int e = es_launch_scan(L, (int)layout, (int)tn.count_stages, I.W, grid, c->stream);
     if (e) return cuda_fail((cudaError_t)e, "scan launch");
     c->launched = true;
     return ES_OK;
@@ -881,7 +903,11 @@ int es_batch_create(es_ctx* const* ctxs, uint32_t n_ctx, const es_batch_item* it
         }
         es_batch::Sub sub;
         sub.words = cls == 0 ? 0u : (cls == 4 && words == 0 ? 4u : (words ? words : cls));
-        const SmemPlan sp = plan_smem(small_max, nf_max, tune);
+        uint32_t stage_words = 0;   // the largest inner-stage tables among the class's plans
+        for (uint32_t j = pos; j < end; ++j)
+            stage_words = std::max<uint32_t>(stage_words, ctxs[items[order[j]].ctx_index]->h_inst.mask_off[F]);
+        sub.layout = launch_layout(tune.layout, sub.words, small_max, nf_max, tune, stage_words);
+        const SmemPlan sp = plan_smem(small_max, nf_max, tune, sub.layout == ES_LAYOUT_SMEM ? stage_words : 0u);
         EsLaunch& L = sub.L;
         memset(&L, 0, sizeof(L));
         L.items = b->d_items_launch + pos;
@@ -901,7 +927,8 @@ int es_batch_create(es_ctx* const* ctxs, uint32_t n_ctx, const es_batch_item* it
         L.smem_bytes = sp.bytes;
         L.cnt_off = sp.cnt_off;
         L.queue_off = sp.queue_off;
-        if (int e = grid_for(tune.layout, tune.count_stages, sub.words, F, tune, sp.bytes,
+        L.stage_off = sp.stage_off;
+        if (int e = grid_for(sub.layout, tune.count_stages, sub.words, F, tune, sp.bytes,
                              std::max<uint64_t>(units, 1), &sub.grid)) {
             es_batch_destroy(b);
             return e;
@@ -927,7 +954,7 @@ static int batch_enqueue(es_batch* b) {
         ES_CUDA(cudaMemsetAsync(b->d_counts, 0, 8ull * b->counts_words, b->stream), "memset");
     for (const es_batch::Sub& sub : b->subs) {
         if (!sub.L.total_units) continue;
-        int e = es_launch_scan(sub.L, (int)b->tune.layout, (int)b->tune.count_stages, sub.words, sub.grid, b->stream);
+        int e = es_launch_scan(sub.L, (int)sub.layout, (int)b->tune.count_stages, sub.words, sub.grid, b->stream);
         if (e) return cuda_fail((cudaError_t)e, "scan launch");
     }
     // survivors carry the caller's item index: the min-reduction reads the items in that order
@@ -1126,7 +1153,10 @@ extern "C" int es_search_blocks_static(const es_ctx* c, uint64_t t0, uint32_t n_
     const es_tune& tn = c->tune;
     const uint32_t nf = I.n_filters;
     const uint32_t F = stage_filters(tn.layout, tn.mask_filters, nf, I.F_built);
-    const SmemPlan sp = plan_smem((uint32_t)I.small_bytes, nf, tn);
+    es_tune tn0 = tn;
+    tn0.count_stages = 0;   // the static search never counts
+    const uint32_t layout = launch_layout(tn.layout, I.W, I.small_bytes, nf, tn0, I.mask_off[F]);
+    const SmemPlan sp = plan_smem((uint32_t)I.small_bytes, nf, tn0, layout == ES_LAYOUT_SMEM ? I.mask_off[F] : 0u);
     const uint64_t per_unit = 32ull * tn.strip;
     uint64_t cbeg = 0;
     const uint64_t ncyc = cycles_of(I, 0, I.n_outer, &cbeg);
@@ -1176,10 +1206,11 @@ extern "C" int es_search_blocks_static(const es_ctx* c, uint64_t t0, uint32_t n_
     L.smem_bytes = sp.bytes;
     L.cnt_off = sp.cnt_off;
     L.queue_off = sp.queue_off;
+    L.stage_off = sp.stage_off;
     if (L.total_units) {
         int grid = 0;
-        if (int e = grid_for(tn.layout, 0, I.W, F, tn, sp.bytes, L.total_units, &grid)) return e;
-        int e = es_launch_scan(L, (int)tn.layout, 0, I.W, grid, st);
+        if (int e = grid_for(layout, 0, I.W, F, tn, sp.bytes, L.total_units, &grid)) return e;
+        int e = es_launch_scan(L, (int)layout, 0, I.W, grid, st);
         if (e) return cuda_fail((cudaError_t)e, "scan launch");
     }
     int e = es_launch_min(d_out, d_count, out_cap, d_items, 1, d_found, d_min, st);

@@ -103,17 +103,20 @@ struct EsLaunch {
     uint32_t smem_bytes;              // dynamic shared memory of the launch
     uint32_t cnt_off;                 // byte offset of the per-warp tail-stage counters in smem
     uint32_t queue_off;               // byte offset of the per-warp survivor queues in smem
+    uint32_t stage_off;               // byte offset of the staged phase tables (ES_LAYOUT_SMEM)
     // single-plan launches carry their one item and block constants by value
     EsItem item0;
     uint32_t tconst0[ES_MAX_FILTERS];
 };
 
-// Scan kernel instances by layout (es_scan_wm.cu / es_scan_wmc.cu, es_scan_pair.cu, es_scan_sc.cu).
+// Scan kernel instances by layout (es_scan_wm.cu / es_scan_wmc.cu, es_scan_pair.cu, es_scan_sc.cu,
+// es_scan_sm.cu).
 typedef void (*ScanFn)(const EsLaunch);
 ScanFn es_pick_wordmask_fast(uint32_t words, uint32_t mask_filters);
 ScanFn es_pick_wordmask_count(uint32_t words, uint32_t mask_filters);
 ScanFn es_pick_pair(int count, uint32_t words, uint32_t mask_filters);
 ScanFn es_pick_scalar(int count, uint32_t mask_filters);
+ScanFn es_pick_smem(int count, uint32_t words, uint32_t mask_filters);
 
 // Host-side launchers implemented in es_scan.cu (return a cudaError_t value).
 int es_scan_prepare(int smem_optin_bytes);
@@ -129,3 +132,7 @@ int es_launch_min(const struct es_survivor* surv, const unsigned long long* surv
                   void* stream);
 // mix = 0: ALU-pipe probe (IADD3 + LOP3); mix = 1: ALU + FMA-pipe probe (LOP3 + IMAD)
 int es_launch_int_peak(unsigned long long* sink, int grid, int threads, int iters, int mix, void* stream);
+
+// The library-wide "last error" message of the calling thread (es_last_error), for translation
+// units other than es_abi.cu.
+void es_set_last_error(const char* msg);

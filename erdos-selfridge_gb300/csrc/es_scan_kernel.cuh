@@ -27,8 +27,11 @@
 //  * Inner ring: its terms are sorted once on the host, so the wrap (s >= M) is a suffix of the
 //    sorted slots; its start (the carry split) comes from 32-bit keys through a 512-bucket
 //    table.  Word-mask layout: a filter costs two phase-table loads, P_f[phase] and the row a
-//    wrap selects, per word (or per 16-byte row of up to four words); pair layout: one load
-//    that holds both rows; scalar layout: one residue + bit test per live candidate.
+//    wrap selects, per word (or per 16-byte row of up to four words); the shared-memory layout
+//    is the same with the inner-stage filters' tables copied into shared memory at launch (the
+//    random 4- or 8-byte gathers then cost a few bank wavefronts instead of one L1 sector per
+//    lane); pair layout: one load that holds both rows; scalar layout: one residue + bit test
+//    per live candidate.
 //  * Inner words that still hold candidates after the inner-ring stage are queued per warp as
 //    one 16-byte entry per lane; a flush takes 32 entries, one candidate per lane (full warps,
 //    not single lanes), runs the next filters from 32-bit term residues, and gives only the
@@ -110,6 +113,19 @@ __device__ __forceinline__ uint32_t mod128(const U4 x, const EsFilterC& f) {
 __device__ __forceinline__ uint32_t red1(uint32_t v, uint32_t q) { return min(v, v - q); }
 // v mod q for v < 3q
 __device__ __forceinline__ uint32_t red2(uint32_t v, uint32_t q) { return red1(red1(v, q), q); }
+
+// Phase-table loads: through L1 (read-only path) for tables in global memory, or from shared
+// memory (a 32-bit shared address) when the launch staged the tables there (ES_LAYOUT_SMEM).
+__device__ __forceinline__ uint32_t lds32(uint32_t saddr) {
+    uint32_t v;
+    asm("ld.shared.u32 %0, [%1];" : "=r"(v) : "r"(saddr));
+    return v;
+}
+__device__ __forceinline__ uint2 lds64(uint32_t saddr) {
+    uint2 v;
+    asm("ld.shared.v2.u32 {%0, %1}, [%2];" : "=r"(v.x), "=r"(v.y) : "r"(saddr));
+    return v;
+}
 
 // Volatile shared loads: values the ring-1 sweep needs only on its rare paths are re-read where
 // they are used instead of being held in registers across the sweep.
@@ -404,8 +420,11 @@ __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, u
     }
     __syncwarp();
     constexpr int FA = F > 0 ? F : 1;   // array extent
+    // word-mask phase tables, in global memory or staged in shared memory by the launch
+    constexpr bool WMASK = LAYOUT == ES_LAYOUT_WORDMASK || LAYOUT == ES_LAYOUT_SMEM;
     uint32_t qf[FA], corr[FA];
     const uint32_t* tab[FA];
+    uint32_t tabs[FA];   // shared address of each staged table (ES_LAYOUT_SMEM)
 #pragma unroll
     for (int f = 0; f < F; ++f) {
         const bool on = (uint32_t)f < Feff;
@@ -414,6 +433,7 @@ __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, u
         tab[f] = LAYOUT == ES_LAYOUT_WORDMASK ? masks_g + si.mask_off[f]
                  : LAYOUT == ES_LAYOUT_PAIR   ? si.pairs + 2u * si.mask_off[f]
                                               : si.allowed + (on ? sFC[f].off : 0u);
+        tabs[f] = (uint32_t)__cvta_generic_to_shared(smem + L.stage_off) + 4u * si.mask_off[f];
     }
     uint32_t cnt[FA];
 #pragma unroll
@@ -563,7 +583,7 @@ __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, u
                 if (has) push<COUNT>(Q, smem, si, lane, step, qhead, qsize, has, b0, b1, split, d1, 0u, wm1);
                 continue;
             }
-            if (LAYOUT == ES_LAYOUT_WORDMASK && WT == 4) {
+            if (WMASK && WT == 4) {
                 // three or four inner words: rows padded to four words, so each side of the
                 // carry split is one 16-byte load per filter; two pair entries per outer index
                 uint32_t b[4], cmw[4];
@@ -591,7 +611,7 @@ __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, u
                 if (h1) push<COUNT>(Q, smem, si, lane, step, qhead, qsize, h1, b[2], b[3], split, d1, 2u, wm1);
                 continue;
             }
-            if (LAYOUT == ES_LAYOUT_WORDMASK && WT == 2) {
+            if (WMASK && WT == 2) {
                 // two inner words: both words of a phase are adjacent in P_f, so one 8-byte load
                 // per filter and phase serves them, and the pair is queued as one entry
                 uint32_t b0 = act ? 0xffffffffu : 0u, b1 = act ? tail : 0u;
@@ -601,8 +621,10 @@ __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, u
                 for (int f = 0; f < F; ++f) {
                     const uint32_t x0 = red2(BQ2[f] + tq[f] + (corr[f] & wm1), qf[f]);
                     const uint32_t x1 = red1(x0 + corr[f], qf[f]);
-                    const uint2 m0 = __ldg(reinterpret_cast<const uint2*>(tab[f]) + x0);
-                    const uint2 m1 = __ldg(reinterpret_cast<const uint2*>(tab[f]) + x1);
+                    const uint2 m0 = LAYOUT == ES_LAYOUT_SMEM ? lds64(tabs[f] + 8u * x0)
+                                                              : __ldg(reinterpret_cast<const uint2*>(tab[f]) + x0);
+                    const uint2 m1 = LAYOUT == ES_LAYOUT_SMEM ? lds64(tabs[f] + 8u * x1)
+                                                              : __ldg(reinterpret_cast<const uint2*>(tab[f]) + x1);
                     b0 &= (m0.x & ~cm0) | (m1.x & cm0);
                     b1 &= (m0.y & ~cm1) | (m1.y & cm1);
                     if (COUNT) cnt[f] += __popc(b0) + __popc(b1);
@@ -618,14 +640,16 @@ __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, u
                 const uint32_t base = wd << 5;
                 // slots >= split of this word wrap: all-ones shifted left by (split - base) in [0, 32]
                 const uint32_t cm = __funnelshift_lc(0u, 0xffffffffu, max(split, base) - base) & valid;
-                if (LAYOUT == ES_LAYOUT_WORDMASK) {
+                if (WMASK) {
                     // straight-line cascade: two table loads per filter per 32 candidates
 #pragma unroll
                     for (int f = 0; f < F; ++f) {
                         const uint32_t x0 = red2(BQ2[f] + tq[f] + (corr[f] & wm1), qf[f]);   // n mod q_f, ring-0 base
                         const uint32_t x1 = red1(x0 + corr[f], qf[f]);                      // the same after a wrap
-                        const uint32_t m0 = __ldg(tab[f] + x0 * RSn + wd);
-                        const uint32_t m1 = __ldg(tab[f] + x1 * RSn + wd);
+                        const uint32_t m0 = LAYOUT == ES_LAYOUT_SMEM ? lds32(tabs[f] + 4u * (x0 * RSn + wd))
+                                                                     : __ldg(tab[f] + x0 * RSn + wd);
+                        const uint32_t m1 = LAYOUT == ES_LAYOUT_SMEM ? lds32(tabs[f] + 4u * (x1 * RSn + wd))
+                                                                     : __ldg(tab[f] + x1 * RSn + wd);
                         bits &= (m0 & ~cm) | (m1 & cm);
                         if (COUNT) cnt[f] += __popc(bits);
                     }
@@ -718,6 +742,8 @@ __global__ void __launch_bounds__(ES_LB_THREADS, ES_LB_MINB) es_scan_kernel(cons
         if (tid == 0) si = *items[0].inst;
         __syncthreads();
         copy_words(reinterpret_cast<uint32_t*>(smem), reinterpret_cast<const uint32_t*>(si.small), si.small_bytes >> 2);
+        if (LAYOUT == ES_LAYOUT_SMEM)   // the inner-stage filters' phase tables (16-byte aligned)
+            copy_words(reinterpret_cast<uint32_t*>(smem + L.stage_off), si.masks, si.mask_off[F]);
         __syncthreads();
         for (;;) {
             unsigned long long w = 0;
@@ -774,6 +800,8 @@ __global__ void __launch_bounds__(ES_LB_THREADS, ES_LB_MINB) es_scan_kernel(cons
             __syncthreads();
             copy_words(reinterpret_cast<uint32_t*>(smem), reinterpret_cast<const uint32_t*>(si.small),
                        si.small_bytes >> 2);
+            if (LAYOUT == ES_LAYOUT_SMEM)
+                copy_words(reinterpret_cast<uint32_t*>(smem + L.stage_off), si.masks, si.mask_off[F]);
             __syncthreads();
             cur_inst = item.inst_id;
         }

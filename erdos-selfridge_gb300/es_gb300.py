@@ -48,7 +48,7 @@ from es_plan import TUNABLES as _PLAN_TUNABLES  # noqa: E402
 TUNABLES = dict(_PLAN_TUNABLES)
 TUNABLES.update({
     "chunk_log2": 34,        # positions per _launch chunk issued by scan_block
-    "layout": "auto",        # "auto" (pair or word-mask by table bytes) | "wordmask" | "pair" | "scalar"
+    "layout": "auto",        # "auto" (by table bytes) | "wordmask" | "pair" | "smem" | "scalar"
     "threads": 512,          # CTA size
     "strip": 2,              # ring-1 cycles per lane per warp-unit
     "smem_kb": 0,            # accepted, no effect (phase tables are read through L1)
@@ -74,7 +74,7 @@ def _tune_from(tun: dict, plan=None) -> N.Tune:
     if layout == "auto":
         code = N.layout_for_plan(plan, F) if plan is not None else N.LAYOUT_WORDMASK
     else:
-        code = {"scalar": N.LAYOUT_SCALAR, "pair": N.LAYOUT_PAIR}.get(layout, N.LAYOUT_WORDMASK)
+        code = {"scalar": N.LAYOUT_SCALAR, "pair": N.LAYOUT_PAIR, "smem": N.LAYOUT_SMEM}.get(layout, N.LAYOUT_WORDMASK)
     return N.make_tune(layout=code, mask_filters=F,
                        threads=int(tun.get("threads", 512)), strip=int(tun.get("strip", 2)),
                        smem_kb=int(tun.get("smem_kb", 0)), ctas_per_sm=int(tun.get("ctas_per_sm", 4)),
@@ -200,8 +200,8 @@ class GpuSieve:
         self.ochunk = max(1, self.chunk // self.r0)
         self.launches = 0
         self.residues_checked = 0
-        self.mask_mode = {N.LAYOUT_SCALAR: "scalar-gb300", N.LAYOUT_PAIR: "pair-gb300"}.get(
-            self.tune.layout, "wordmask-gb300")
+        self.mask_mode = {N.LAYOUT_SCALAR: "scalar-gb300", N.LAYOUT_PAIR: "pair-gb300",
+                          N.LAYOUT_SMEM: "smem-gb300"}.get(self.tune.layout, "wordmask-gb300")
         self.tconst = _Tconst(self)
         self.out_n = _OutN(self)
         self.out = _Out(self)

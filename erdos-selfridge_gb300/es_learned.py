@@ -536,10 +536,24 @@ def main():
     ap.add_argument("--out", default=None)
     ap.add_argument("--epochs", type=int, default=600)
     ap.add_argument("--save-model", default=None, help="write the trained model (JSON) here")
+    ap.add_argument("--eval-model", default=None,
+                    help="score this trained model on the held-out k only (probes just those k)")
     a = ap.parse_args()
     rng = np.random.default_rng(0)
     ks = sorted(int(x) for x in rng.choice(np.arange(100, 401), size=a.n_k, replace=False))
     t0 = time.time()
+    if a.eval_model:
+        _, test_ks = split_ks(ks, a.held_out)
+        rows = collect(test_ks, log=lambda s: print(s, file=sys.stderr, flush=True))
+        if a.dataset:
+            json.dump(rows, open(a.dataset, "w"))
+        rep = evaluate(rows, CostModel.load(a.eval_model), set(test_ks))
+        rep.update({"rows": len(rows), "probe_s": time.time() - t0, "model": a.eval_model})
+        s = json.dumps(rep)
+        if a.out:
+            open(a.out, "w").write(s + "\n")
+        print(s)
+        return
     if a.dataset and os.path.exists(a.dataset):
         rows = json.load(open(a.dataset))
     else:

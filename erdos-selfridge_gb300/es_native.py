@@ -20,6 +20,7 @@ ES_ERR_OVERFLOW = -3
 LAYOUT_WORDMASK = 0
 LAYOUT_SCALAR = 1
 LAYOUT_PAIR = 2       # word masks with the wrapped row beside each phase (inner rings <= 64 slots)
+LAYOUT_SMEM = 3       # word masks of the inner-stage filters staged in shared memory (<= 64 slots)
 MAX_MASK_FILTERS = 8
 
 
@@ -181,19 +182,26 @@ class PlanArrays:
 # L1 bytes the phase tables can count on beside the scan's ~51 KB of shared memory (each SM has
 # 256 KB for L1 and shared memory together; the CUDA driver's carveout for the scan is 64 KB)
 L1_TABLE_BUDGET = 180 * 1024
+# Shared-memory bytes the inner-stage phase tables can take: a CTA may opt in to 227 KB, of which
+# the scan's small tables and per-warp queues take about 55 KB at 512 threads (the library checks
+# the exact figure per launch and falls back to the word-mask layout when the tables do not fit)
+SMEM_TABLE_BUDGET = 171 * 1024
 
 
 def layout_for(r0: int, filter_q, mask_filters: int) -> int:
     """Table layout of the inner-ring stage for an inner ring of r0 slots whose first filters have
-    moduli filter_q.  Pair tables cost one load per filter and word instead of two, but twice the
-    bytes: they win unless the word-mask tables fit L1 and the pair tables do not (measured on
-    GB300: k = 300 keeps word masks at F = 3..4, k = 390 gains about 1.3x from pairs).  Neither
-    choice changes which candidates pass."""
+    moduli filter_q.  Word-mask tables that fit in shared memory are staged there (a random
+    4- or 8-byte gather from shared memory costs a few bank wavefronts instead of one L1 sector
+    per lane: 1.17x at k = 300).  Otherwise pair tables cost one load per filter and word instead
+    of two, but twice the bytes: they win unless the word-mask tables fit L1 and the pair tables
+    do not (k = 390 gains about 1.3x from pairs).  Neither choice changes which candidates pass."""
     W = -(-max(1, int(r0)) // 32)
     if W > 2:
         return LAYOUT_WORDMASK
     qs = [int(q) for q in list(filter_q)[:min(int(mask_filters), MAX_MASK_FILTERS)]]
     single = 4 * sum(-(-(q * W) // 4) * 4 for q in qs)
+    if single <= SMEM_TABLE_BUDGET:
+        return LAYOUT_SMEM
     if single <= L1_TABLE_BUDGET < 2 * single:
         return LAYOUT_WORDMASK
     return LAYOUT_PAIR

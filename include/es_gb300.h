@@ -42,6 +42,10 @@ extern "C" {
 #define ES_LAYOUT_PAIR 2      /* word-mask tables with each phase's wrapped row beside it: one
                                  load per filter and word (inner rings of <= 64 slots; wider
                                  rings use ES_LAYOUT_WORDMASK) */
+#define ES_LAYOUT_SMEM 3      /* word-mask tables of the inner-stage filters copied into shared
+                                 memory by every CTA at launch (inner rings of <= 64 slots whose
+                                 tables fit beside the scan's own shared memory; otherwise the
+                                 launch uses ES_LAYOUT_WORDMASK) */
 
 #define ES_MAX_MASK_FILTERS 8 /* filters evaluated in the inner-ring stage */
 #define ES_MAX_Q (1u << 20)   /* filter moduli q = p^t_p must be below 2^20 (k <= 1024) */
@@ -73,7 +77,7 @@ typedef struct es_plan_desc {
 /* Launch shape and table layout; chosen by the autotuner (es_autotune.py).  None of these
  * changes which candidates pass. */
 typedef struct es_tune {
-    uint32_t layout;        /* ES_LAYOUT_WORDMASK, ES_LAYOUT_SCALAR or ES_LAYOUT_PAIR */
+    uint32_t layout;        /* ES_LAYOUT_WORDMASK, ES_LAYOUT_SCALAR, ES_LAYOUT_PAIR or ES_LAYOUT_SMEM */
     uint32_t mask_filters;  /* filters in the inner-ring stage, 1..ES_MAX_MASK_FILTERS */
     uint32_t threads;       /* CTA size, multiple of 32 in [64, 512] */
     uint32_t strip;         /* ring-1 cycles per thread per work unit (strip depth) */
@@ -198,6 +202,47 @@ int es_batch_destroy(es_batch* b);
 int es_search_blocks_static(const es_ctx* ctx, uint64_t t0, uint32_t n_blocks, es_survivor* d_out,
                             uint64_t out_cap, unsigned long long* d_count, unsigned long long* d_min,
                             void* stream);
+
+/* ---- meet-in-the-middle search ------------------------------------------------------------
+ * Replaces the CuPy kernel and driver of sieve/gpu_mitm.py:33-219 (the derivation is
+ * harness/mitm_search.py:1-25).  Wheel residues n = (s1 + s2) mod M: s1 sums one term per ring of
+ * the large half (decoded from its index in the kernel), s2 one per ring of the small half (held
+ * sorted on the device with a directory over its top bits).  A scan tests every n < B of the s1
+ * indices given against the residual filters in order and keeps the survivors. */
+typedef struct es_mitm es_mitm;
+typedef struct es_mitm_desc {
+    uint32_t k;
+    uint32_t n_rings1;          /* rings of the large half S1 (<= 32), decoded in the kernel */
+    uint32_t n_rings2;          /* rings of the small half S2 (<= 32), materialised and sorted */
+    uint32_t n_filters;
+    uint64_t M_lo, M_hi;        /* wheel modulus, 2 <= M < 2^126 */
+    const uint32_t* radix1;     /* [n_rings1] residues per ring */
+    const uint64_t* term1_lo;   /* [sum radix1] a * c_p mod M, low 64 bits */
+    const uint64_t* term1_hi;
+    const uint32_t* radix2;     /* [n_rings2]; |S2| = prod radix2 must stay below 2^31 */
+    const uint64_t* term2_lo;
+    const uint64_t* term2_hi;
+    const uint32_t* filter_q;   /* [n_filters] residual moduli in cascade order */
+    const uint32_t* allowed;    /* packed admissible-residue bits, ceil(q/32) words each */
+} es_mitm_desc;
+/* Builds S2 (every sum mod M, sorted) and its directory on the host and uploads all tables. */
+int es_mitm_create(const es_mitm_desc* desc, es_mitm** out);
+int es_mitm_destroy(es_mitm* m);
+int es_mitm_info(const es_mitm* m, uint64_t* n1, uint64_t* n2);
+/* Survivor capacity (default 2^20 records); the reference's out_cap (sieve/gpu_mitm.py:133). */
+int es_mitm_set_capacity(es_mitm* m, uint64_t cap);
+/* Zeroes the survivor and candidate counters (the reference's d_on.fill(0), gpu_mitm.py:193). */
+int es_mitm_reset(es_mitm* m);
+/* Every n < B (1 <= B <= M) with s1 index in [s1_begin, s1_end) through the cascade;
+ * asynchronous; survivors and the count of n tested accumulate until es_mitm_reset.  A bound
+ * with lo + B >= M for lo = (M - s1) mod M wraps to the front of S2 (B = M covers all of S2),
+ * as the reference kernel does (gpu_mitm.py:78-85). */
+int es_mitm_scan(es_mitm* m, uint64_t B_lo, uint64_t B_hi, uint64_t s1_begin, uint64_t s1_end);
+/* Synchronises; survivors as n = n_hi * 2^64 + n_lo in device order, their count and the count
+ * of n tested.  ES_ERR_OVERFLOW when the count exceeded the capacity (the reference's
+ * SURVIVOR_OVERFLOW, gpu_mitm.py:203-204). */
+int es_mitm_results(es_mitm* m, uint64_t* n_lo, uint64_t* n_hi, uint64_t cap, uint64_t* n_surv,
+                    uint64_t* n_cand);
 
 /* ---- learned planner: 3-layer FP32 MLP trained and evaluated by this library's kernels -------
  * No counterpart in the reference: it stands in for the knapsack planner's analytic cost

@@ -9,7 +9,8 @@ survivor and the terminal minimum g(k).
 
 It imports the reference, so it runs only where the reference is checked out:
 
-    python tests/golden/check_replays_with_reference.py --ref /root/reference
+    python tests/golden/check_replays_with_reference.py --ref <reference checkout>
+    (or set ES_REFERENCE_ROOT)
 """
 from __future__ import annotations
 
@@ -24,7 +25,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 
 def main() -> int:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("ES_REFERENCE_ROOT"),
+                    required="ES_REFERENCE_ROOT" not in os.environ,
+                    help="reference checkout (default: $ES_REFERENCE_ROOT)")
     a = ap.parse_args()
     sys.path.insert(0, a.ref)
     spec = importlib.util.spec_from_file_location("verify_release", os.path.join(a.ref, "harness", "verify_release.py"))

@@ -1,9 +1,10 @@
 #!/usr/bin/env python3
 """Generate the golden fixtures in tests/golden from the reference project's own code.
 
-Run in a container where the reference checkout is mounted (default /root/reference):
+Run where the reference checkout is available; its location comes from --ref or the
+ES_REFERENCE_ROOT environment variable (one of them is required):
 
-    python tests/golden/make_golden.py [--ref /root/reference] [--jobs 8]
+    python tests/golden/make_golden.py --ref <reference checkout> [--jobs 8]
 
 Everything written here comes from the reference's CPU path, never from this repository:
 
@@ -164,7 +165,9 @@ def batch_instances(seed: int = 0, count: int = 64):
 
 def main() -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("ES_REFERENCE_ROOT"),
+                    required="ES_REFERENCE_ROOT" not in os.environ,
+                    help="reference checkout (default: $ES_REFERENCE_ROOT)")
     ap.add_argument("--jobs", type=int, default=os.cpu_count() or 4)
     ap.add_argument("--only", default="", help="comma list of fixtures to (re)build")
     a = ap.parse_args()

@@ -26,12 +26,13 @@ def test_library_exports_every_declared_symbol():
 
 
 def test_binding_covers_the_header():
-    """The Python bindings (es_native: engine; es_learned: MLP) cover every entry point except
-    the one the no-allocation test binds itself."""
+    """The Python bindings (es_native: engine; es_learned: MLP; es_mitm: meet-in-the-middle)
+    cover every entry point except the one the no-allocation test binds itself."""
     import es_learned
+    import es_mitm
     import es_native
     es_native.lib()
-    src = open(es_native.__file__).read() + open(es_learned.__file__).read()
+    src = open(es_native.__file__).read() + open(es_learned.__file__).read() + open(es_mitm.__file__).read()
     missing = [n for n in _declared() if n not in src and n != "es_search_blocks_static"]
     assert not missing, missing
 

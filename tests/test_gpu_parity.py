@@ -22,6 +22,8 @@ SHAPES = [
     dict(layout=1, mask_filters=6, threads=96, strip=2, smem_kb=16),
     dict(layout=2, mask_filters=4, threads=256, strip=2),
     dict(layout=2, mask_filters=3, threads=512, strip=5),
+    dict(layout=3, mask_filters=4, threads=512, strip=2),
+    dict(layout=3, mask_filters=6, threads=256, strip=3),
 ]
 
 
@@ -68,7 +70,7 @@ def test_k300_seeded_sample(native):
     plan = es_gb300.Plan(300)
     assert [[p, T] for p, T in plan.wheel] == g["plan"]["wheel"]
     outer = _sample(g["seed"], g["domain"], g["draws"], g["outer_sha256"])
-    for shape in (SHAPES[0], SHAPES[3], SHAPES[5], dict(layout=0, mask_filters=8, threads=512, strip=16)):
+    for shape in (SHAPES[0], SHAPES[3], SHAPES[5], SHAPES[7], dict(layout=0, mask_filters=8, threads=512, strip=16)):
         ctx = N.Context(plan, _tune(N, **shape))
         ctx.set_block(0)
         ctx.reset()
@@ -88,7 +90,8 @@ def test_k390_seeded_sample(native, role):
     plan = es_gb300.Plan(390, None, g["wheel"])
     assert str(plan.M) == g["plan"]["M"] and plan.rest == g["plan"]["rest"]
     outer = _sample(g["seed"], g["domain"], g["draws"], g["outer_sha256"])
-    for shape in (dict(mask_filters=8), dict(layout=2, mask_filters=4), dict(layout=2, mask_filters=3, strip=1)):
+    for shape in (dict(mask_filters=8), dict(layout=2, mask_filters=4), dict(layout=2, mask_filters=3, strip=1),
+                  dict(layout=3, mask_filters=2)):
         ctx = N.Context(plan, _tune(N, **shape))
         ctx.set_block(0)
         ctx.reset()

@@ -71,39 +71,22 @@ def test_load_known(tmp_path):
 
 
 def test_layout_rule():
-    """The default table layout: word masks where they fit L1 and pair tables would not (k = 300
-    at F = 3..4), pair tables where neither fits (k = 390) or both fit, word masks for inner rings
-    wider than two words; "auto" in the drop-in tunables resolves through it."""
+    """The default table layout: word masks staged in shared memory where the inner-stage tables
+    fit (k = 300 at F = 2..4), else pair tables where the word masks do not fit L1 (k = 300 at
+    F = 5, k = 390), word masks for inner rings wider than two words; "auto" in the drop-in
+    tunables resolves through it."""
     import es_gb300
     import es_native as N
     P300 = es_gb300.Plan(300)
-    assert N.layout_for_plan(P300, 4) == N.LAYOUT_WORDMASK
-    assert N.layout_for_plan(P300, 3) == N.LAYOUT_WORDMASK
+    assert N.layout_for_plan(P300, 4) == N.LAYOUT_SMEM
+    assert N.layout_for_plan(P300, 3) == N.LAYOUT_SMEM
+    assert N.layout_for_plan(P300, 2) == N.LAYOUT_SMEM
     assert N.layout_for_plan(P300, 5) == N.LAYOUT_PAIR
-    assert N.layout_for_plan(P300, 2) == N.LAYOUT_PAIR
     wheel = [[3, 6], [2, 9], [211, 1], [139, 1], [103, 1], [137, 1], [101, 1], [67, 1], [5, 2],
              [199, 1], [23, 2], [79, 1], [197, 1], [131, 1], [7, 2], [17, 1]]
     assert N.layout_for_plan(es_gb300.Plan(390, None, wheel), 4) == N.LAYOUT_PAIR
     assert N.layout_for(96, [1009, 1013], 2) == N.LAYOUT_WORDMASK
-    assert es_gb300._tune_from(dict(es_gb300.TUNABLES), P300).layout == N.LAYOUT_WORDMASK
+    assert N.layout_for(48, [30011, 30013, 30047], 3) == N.LAYOUT_PAIR   # 720 KB of word masks
+    assert es_gb300._tune_from(dict(es_gb300.TUNABLES), P300).layout == N.LAYOUT_SMEM
     assert es_gb300._tune_from(dict(es_gb300.TUNABLES, layout="scalar"), P300).layout == N.LAYOUT_SCALAR
-
-
-class _OverflowBatch(FakeBatch):
-    """A multi-block search launch whose survivor buffer overflowed (es_batch_group_min's
-    ES_ERR_OVERFLOW): the stored records may miss the least good survivor."""
-
-    def group_min(self, g):
-        import es_native as N
-        raise N.EsError(N.ES_ERR_OVERFLOW, "survivor buffer overflow in the batch")
-
-
-def test_batch_overflow_rescans_block_by_block(monkeypatch, bfile):
-    """An overflowing multi-block launch must not skip the block holding the answer: the search
-    rescans from the same block one block at a time (g(30) lies in block 9)."""
-    import es_gb300
-    sieve, fake = _sieve(monkeypatch, 30)
-    monkeypatch.setattr(es_gb300.N, "Batch", _OverflowBatch)
-    res = sieve.search(None)
-    assert res["status"] == "FOUND" and res["g"] == bfile[30] and res["block"] == 9
-    assert res["residues_checked"] == 10 * sieve.plan.R
+    assert es_gb300._tune_from(dict(es_gb300.TUNABLES, layout="wordmask"), P300).layout == N.LAYOUT_WORDMASK
