@@ -491,9 +491,9 @@ def evaluate(rows, model: CostModel, test_ks, margin: float = VETO_LOG_MARGIN) -
     geo_fixed = math.exp(statistics.fmean(math.log(x) for x in fixed)) if fixed else None
     n_fixed = len(fixed)
 
-    def geo(v):
+    def geomean(v):
         return math.exp(statistics.fmean(math.log(x) for x in v)) if v else None
-    families = {name: geo(list(v.values())) for name, v in family.items() if len(v) == n_fixed}
+    families = {name: geomean(list(v.values())) for name, v in family.items() if len(v) == n_fixed}
     fixed_only = {n: g for n, g in families.items() if n != "analytic-model-choice"}
     best_family = max(fixed_only, key=fixed_only.get) if fixed_only else None
     return {"held_out_k": sorted(by_k), "n_candidates": sum(len(v) for v in by_k.values()),
