@@ -12,6 +12,7 @@
   replayed from a CUDA graph, launch shape from the autotuner, against one launch per instance.
 * replay: whole blocks of recorded frontier wheels (k = 378..400), each compared with the
   reference driver's recorded audit record (survivor counts and sha256 of the survivors).
+* mitm: the meet-in-the-middle search for a few k, with the scan kernel's candidate rate.
 * k390: the two recorded k = 390 wheels (primary and confirmation of evidence/through400/
   runs.json) over positions [0, 2^40) of block 0 in one persistent launch; every survivor of
   either wheel that the other wheel's scanned prefix covers must be a survivor there too.
@@ -204,6 +205,32 @@ def k390_learned(model_path: str, log2_positions: int = 40, reps: int = 2, autot
             "learned": learned, "analytic": analytic}
 
 
+def mitm(ks, mem_gb: float = 8.0, bound_mult: float = 3.0) -> dict:
+    """The meet-in-the-middle search per k (es_mitm.mitm_gpu) with its wall time, and the scan
+    kernel alone on the final round's bound: candidates tested per second of device time."""
+    import es_mitm
+    out = {}
+    for k in ks:
+        t0 = time.perf_counter()
+        r = es_mitm.mitm_gpu(k, mem_gb, bound_mult)
+        wall = time.perf_counter() - t0
+        row = {"status": r["status"], "g": r.get("g"), "wall_s": wall, "M_bits": r.get("M_bits"),
+               "S1": r.get("S1"), "S2": r.get("S2"), "candidates": r.get("candidates")}
+        if r["status"] == "FOUND":
+            P = es_mitm.MitmPlan(k, mem_gb)
+            eng = es_mitm.MitmEngine(P)
+            eng.scan(r["bound"])                      # warm
+            t1 = time.perf_counter()
+            _, cand = eng.scan(r["bound"])
+            dt = time.perf_counter() - t1
+            eng.close()
+            row.update({"final_bound": str(r["bound"]), "final_round_candidates": cand,
+                        "final_round_s": dt, "Gcand_s": cand / dt / 1e9 if dt else None,
+                        "s1_per_s": P.n1 / dt if dt else None})
+        out[k] = row
+    return {"cases": out, "mem_gb": mem_gb, "bound_mult": bound_mult}
+
+
 AUDIT_FIELDS = ("residues_enumerated", "kernel_survivors", "after_n_gt_k_plus_1", "passed_ref_is_good",
                 "sha256_survivors")
 
@@ -232,7 +259,8 @@ def replay(cases, chunk_log2: int = 40) -> dict:
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("which", choices=["small-k", "batch64", "k390", "k390-learned", "replay"])
+    ap.add_argument("which", choices=["small-k", "batch64", "k390", "k390-learned", "replay", "mitm"])
+    ap.add_argument("--k", type=int, nargs="*", default=[140, 150, 160, 170], help="mitm: the k to search")
     ap.add_argument("--cases-file", default=None, help="recorded block audits (replay), JSON {cases: [...]}")
     ap.add_argument("--select", default=None, help="replay: comma list of k:role:t to run")
     ap.add_argument("--model", default=None, help="learned cost model (es_learned.py --save-model)")
@@ -248,6 +276,8 @@ def main():
         out = batch64(autotune=not a.no_autotune)
     elif a.which == "k390":
         out = k390(a.log2_positions)
+    elif a.which == "mitm":
+        out = mitm(a.k)
     elif a.which == "k390-learned":
         out = k390_learned(a.model, a.log2_positions, autotune=not a.no_autotune)
     else:

@@ -191,7 +191,7 @@ WHEEL_TUNES = [
 ]
 
 
-def _orders(plan, rng, shuffles: int = 2) -> list[tuple[str, list[int]]]:
+def _orders(plan, rng, shuffles: int = 2, unique: bool = True) -> list[tuple[str, list[int]]]:
     """Cascade-order families: the reference order, orders that trade rejection against the
     word-mask table footprint (several L1 budgets, two of them sized for pair tables),
     small-q-first heads, and random heads."""
@@ -224,6 +224,8 @@ def _orders(plan, rng, shuffles: int = 2) -> list[tuple[str, list[int]]]:
         perm = ref[:8]
         rng.shuffle(perm)
         out.append((f"shuffle{i}", perm + ref[8:]))
+    if not unique:
+        return out
     seen, uniq = set(), []
     for name, o in out:
         key = tuple(o)
@@ -441,7 +443,7 @@ def evaluate(rows, model: CostModel, test_ks, margin: float = VETO_LOG_MARGIN) -
             by_k.setdefault(r["k"], []).append(r)
     # the analytic model's rate: the geometric-mean throughput of the model's training set
     mean_tp = math.exp(float(model.ym[0]))
-    per_k, err_l, err_a, speed = {}, [], [], []
+    per_k, err_l, err_a, speed, plan_family = {}, [], [], [], {}
     for k, cand in sorted(by_k.items()):
         actual = [c["log_pos"] - c["log_tp"] for c in cand]            # ln(time) up to a constant
         pred_l = model.log_time([c["features"] for c in cand], [c["true_cost"] for c in cand])
@@ -457,6 +459,14 @@ def evaluate(rows, model: CostModel, test_ks, margin: float = VETO_LOG_MARGIN) -
         ib = min(range(len(cand)), key=lambda i: actual[i])           # best measured
         s = math.exp(actual[ia] - actual[il])
         speed.append(s)
+        # ablation of the plan choice: the analytic planner's wheel run with each fixed order
+        # family (the family's order of that wheel, found among the probes by its order)
+        aw = cand[ia]["wheel"]
+        by_order = {tuple(c["order"]): i for i, c in enumerate(cand) if c["wheel"] == aw}
+        for name, order in _orders(es_plan.Plan(k, None, aw), np.random.default_rng(0), shuffles=0, unique=False):
+            j = by_order.get(tuple(order))
+            if j is not None:
+                plan_family.setdefault(name, {})[k] = math.exp(actual[ia] - actual[j])
         per_k[k] = {"analytic": f"{cand[ia]['wheel_name']}/{cand[ia]['order_name']}",
                     "learned": f"{cand[il]['wheel_name']}/{cand[il]['order_name']}",
                     "best": f"{cand[ib]['wheel_name']}/{cand[ib]['order_name']}",
@@ -483,8 +493,14 @@ def evaluate(rows, model: CostModel, test_ks, margin: float = VETO_LOG_MARGIN) -
         fixed.append(dw[il]["gcand"] / ref[0]["gcand"])
         per_k[k]["fixed_scope_learned_order"] = dw[il]["order_name"]
         per_k[k]["fixed_scope_time_ratio"] = fixed[-1]
-        for c in dw:
-            family.setdefault(c["order_name"], {})[k] = c["gcand"] / ref[0]["gcand"]
+        # each named family's order for this wheel (families that coincide with an earlier one
+        # were probed once, under the earlier name) mapped to the probe of that order
+        by_order = {tuple(c["order"]): c for c in dw}
+        P = es_plan.Plan(k, None, dw[0]["wheel"])
+        for name, order in _orders(P, np.random.default_rng(0), shuffles=0, unique=False):
+            c = by_order.get(tuple(order))
+            if c is not None:
+                family.setdefault(name, {})[k] = c["gcand"] / ref[0]["gcand"]
         if "rates" in dw[0]:
             ia = min(range(len(dw)), key=lambda i: _analytic_evals(dw[i]["rates"]))
             family.setdefault("analytic-model-choice", {})[k] = dw[ia]["gcand"] / ref[0]["gcand"]
@@ -496,6 +512,8 @@ def evaluate(rows, model: CostModel, test_ks, margin: float = VETO_LOG_MARGIN) -
     families = {name: geomean(list(v.values())) for name, v in family.items() if len(v) == n_fixed}
     fixed_only = {n: g for n, g in families.items() if n != "analytic-model-choice"}
     best_family = max(fixed_only, key=fixed_only.get) if fixed_only else None
+    plan_families = {name: geomean(list(v.values())) for name, v in plan_family.items() if len(v) == len(speed)}
+    best_plan_family = max(plan_families, key=plan_families.get) if plan_families else None
     return {"held_out_k": sorted(by_k), "n_candidates": sum(len(v) for v in by_k.values()),
             "fixed_scope_geomean_time_ratio_reference_over_learned_order": geo_fixed,
             "fixed_scope_ablation": {
@@ -506,6 +524,11 @@ def evaluate(rows, model: CostModel, test_ks, margin: float = VETO_LOG_MARGIN) -
                 "network_over_analytic_model_choice": (geo_fixed / families["analytic-model-choice"]
                                                        if geo_fixed and families.get("analytic-model-choice")
                                                        else None)},
+            "plan_choice_ablation": {
+                "geomean_time_ratio_analytic_over_analytic_wheel_with_family": plan_families,
+                "best_fixed_family": best_plan_family,
+                "network_over_best_fixed_family": (geo / plan_families[best_plan_family]
+                                                   if best_plan_family and geo else None)},
             "veto_log_margin": margin,
             "mae_log_time_learned": statistics.fmean(err_l) if err_l else None,
             "mae_log_time_analytic": statistics.fmean(err_a) if err_a else None,

@@ -30,7 +30,8 @@ def test_learned_model_beats_analytic_on_held_out_k(native):
 
 def test_packaged_model_on_unseen_k(native):
     """The committed model (trained on 160 k of the seeded 100..400 campaign) on fresh probes of
-    k from that campaign's held-out set: better time predictions than the analytic model."""
+    k from that campaign's held-out set: better time predictions than the analytic model, and
+    plans that finish faster than the analytic planner's."""
     import es_learned
     es_learned.PROBE_LOG2 = 28
     model = es_learned.CostModel.load(es_learned.MODEL_PATH)
@@ -38,7 +39,9 @@ def test_packaged_model_on_unseen_k(native):
     rows = es_learned.collect(held, procs=12)
     rep = es_learned.evaluate(rows, model, set(held))
     assert rep["mae_log_time_learned"] < 0.7 * rep["mae_log_time_analytic"], rep
-    assert rep["geomean_time_ratio_analytic_over_learned"] >= 0.95, rep
+    # the campaign that trained the model measured 1.18x (geomean over these six k) for the
+    # plans the network picks against the analytic planner's; 1.10 leaves room for probe noise
+    assert rep["geomean_time_ratio_analytic_over_learned"] >= 1.10, rep
 
 
 def test_packaged_model_orders_are_permutations(native):
