@@ -43,7 +43,7 @@ import es_plan  # noqa: E402
 
 N_FIRST = 6          # filters described individually in the features
 MODEL_PATH = os.path.join(HERE, "data", "cost_model.json")   # trained on 160 k of 100..400
-FEATURE_DIM = 14 + 3 * N_FIRST
+FEATURE_DIM = 16 + 3 * N_FIRST
 PROBE_LOG2 = 28
 
 
@@ -151,6 +151,12 @@ def features(plan) -> np.ndarray:
          sum(_log2(r) for r in rates) / -64.0,
          _log2(plan._true_cost()) / 64.0,
          (r0 % 32) / 32.0]
+    # the table layout the engine picks for the inner stage (es_native.layout_for, F = 4): staged
+    # in shared memory, pair tables or word masks through L1 -- a step in throughput the table
+    # bytes alone describe only through a sharp threshold
+    import es_native
+    lay = es_native.layout_for(r0, qs, 4)
+    f += [1.0 if lay == es_native.LAYOUT_SMEM else 0.0, 1.0 if lay == es_native.LAYOUT_PAIR else 0.0]
     for j in range(N_FIRST):
         if j < len(qs):
             f += [_log2(qs[j]) / 20.0, rates[j], _log2(qs[j] * W * 4) / 24.0]
