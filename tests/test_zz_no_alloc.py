@@ -37,18 +37,19 @@ def _key(recs, t_max):
                   for r in recs if int(r["t"]) <= t_max)
 
 
-@pytest.mark.parametrize("k,t0,nb,count_stages", [(60, 0, 16, 0), (97, 0, 8, 0), (70, 3, 20, 0), (30, 0, 12, 0),
-                                                  (57, 0, 10, 1)])
-def test_static_search_matches_batch(native, bfile, k, t0, nb, count_stages):
+@pytest.mark.parametrize("k,t0,nb,count_stages,layout", [(60, 0, 16, 0, 0), (97, 0, 8, 0, 0), (70, 3, 20, 0, 0),
+                                                         (30, 0, 12, 0, 0), (57, 0, 10, 1, 0), (97, 0, 8, 0, 3)])
+def test_static_search_matches_batch(native, bfile, k, t0, nb, count_stages, layout):
     """Two calls in a row against the allocating batch path, and the least n against g(k) of the
     b-file (every block before g(k)'s holds no good survivor).  A context built for counting
-    launches works too: the static search never counts."""
+    launches works too (the static search never counts), and so does one whose launches stage
+    the phase tables in shared memory (layout 3)."""
     import torch
     import es_gb300
     N = native
     fn = _entry(N)
     plan = es_gb300.Plan(k)
-    ctx = N.Context(plan, N.make_tune(count_stages=count_stages))
+    ctx = N.Context(plan, N.make_tune(count_stages=count_stages, layout=layout))
     # reference result: the allocating batch path, one group over the same blocks
     b = N.Batch([ctx], [(0, 0, t0 + i, 0, ctx.n_outer) for i in range(nb)], ctx.tune)
     b.run(use_graph=False)
@@ -114,3 +115,25 @@ def test_static_search_rejects_oversize(native):
     rc = fn(ctx.h, 0, MAX_BLOCKS + 1, d_out.data_ptr(), 1024, d_count.data_ptr(), d_min.data_ptr(), None)
     assert rc == -4   # ES_ERR_RANGE
     assert b"n_blocks" in N.lib().es_last_error()
+
+
+def test_static_search_refuses_stream_capture(native):
+    """A call made while its stream is capturing a CUDA graph returns ES_ERR_STATE and enqueues
+    nothing (its descriptor copies come from host staging arrays the next call reuses)."""
+    import torch
+    import es_gb300
+    N = native
+    fn = _entry(N)
+    ctx = N.Context(es_gb300.Plan(40), N.make_tune(count_stages=0))
+    d_out = torch.zeros(1024 * N.SURVIVOR_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+    d_count = torch.zeros(1, dtype=torch.int64, device="cuda")
+    d_min = torch.zeros(4, dtype=torch.int64, device="cuda")
+    s = torch.cuda.Stream()
+    g = torch.cuda.CUDAGraph()
+    torch.cuda.synchronize()
+    with torch.cuda.graph(g, stream=s):
+        rc = fn(ctx.h, 0, 4, d_out.data_ptr(), 1024, d_count.data_ptr(), d_min.data_ptr(),
+                torch.cuda.current_stream().cuda_stream)
+        d_count.add_(0)   # something for the graph to hold
+    assert rc == -6   # ES_ERR_STATE
+    assert b"capturing" in N.lib().es_last_error()
