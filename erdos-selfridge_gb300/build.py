@@ -21,7 +21,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "libes_gb300.so")
 OBJDIR = os.path.join(HERE, "_build")
-SOURCES = ["es_scan_wm.cu", "es_scan_wmc.cu", "es_scan_pair.cu", "es_scan_sc.cu", "es_scan_sm.cu", "es_scan.cu", "es_abi.cu",
+SOURCES = ["es_scan_wm.cu", "es_scan_wmc.cu", "es_scan_pair.cu", "es_scan_sc.cu", "es_scan_sm.cu", "es_scan_sp.cu", "es_scan.cu", "es_abi.cu",
            "es_mlp.cu", "es_mitm.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

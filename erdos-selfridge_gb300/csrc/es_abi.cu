@@ -77,9 +77,9 @@ int device_facts() {
 size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 int check_tune(const es_tune& t) {
-    if (t.layout != ES_LAYOUT_WORDMASK && t.layout != ES_LAYOUT_SCALAR && t.layout != ES_LAYOUT_PAIR &&
-        t.layout != ES_LAYOUT_SMEM)
-        return fail(ES_ERR_ARG, "tune.layout must be 0 (word-mask), 1 (scalar), 2 (pair) or 3 (shared-memory tables)");
+    if (t.layout > ES_LAYOUT_SMEM_PAIR)
+        return fail(ES_ERR_ARG, "tune.layout must be 0 (word-mask), 1 (scalar), 2 (pair), 3 (word masks in shared "
+                                "memory) or 4 (pair tables in shared memory)");
     if (t.mask_filters < 1 || t.mask_filters > ES_MAX_MASK_FILTERS)
         return fail(ES_ERR_ARG, "tune.mask_filters must be in 1..8");
     if (t.threads < 64 || t.threads > 1024 || t.threads % 32)
@@ -95,7 +95,7 @@ es_tune default_tune() {
     t.layout = ES_LAYOUT_WORDMASK;
     t.mask_filters = 4;
     t.threads = 512;
-    t.strip = 2;
+    t.strip = 8;
     t.smem_kb = 0;
     t.ctas_per_sm = 4;
     t.count_stages = 0;
@@ -172,7 +172,8 @@ struct es_batch {
 namespace {
 
 // Shared-memory plan of one launch:
-// [small tables | staged phase tables (ES_LAYOUT_SMEM) | per-warp stage counters | per-warp slots].
+// [small tables | staged phase tables (ES_LAYOUT_SMEM, _SMEM_PAIR) | per-warp stage counters |
+//  per-warp slots].
 struct SmemPlan {
     uint32_t stage_off, cnt_off, queue_off, bytes;
 };
@@ -195,16 +196,25 @@ SmemPlan plan_smem(uint32_t small_max, uint32_t nf_max, const es_tune& tune, uin
     return p;
 }
 
-// The layout a launch actually runs: ES_LAYOUT_SMEM only for inner rings of one or two words
+// Words of inner-stage tables a staged layout copies into shared memory: the word-mask tables of
+// the first F filters (ES_LAYOUT_SMEM) or their pair tables, twice the words (ES_LAYOUT_SMEM_PAIR).
+uint32_t stage_words_of(uint32_t layout, const EsInst& I, uint32_t F) {
+    if (layout == ES_LAYOUT_SMEM) return I.mask_off[F];
+    if (layout == ES_LAYOUT_SMEM_PAIR) return 2u * I.mask_off[F];
+    return 0u;
+}
+
+// The layout a launch actually runs: a staged layout only for inner rings of one or two words
 // whose stage_words of inner-stage tables fit the opt-in shared memory beside the rest of the
-// launch's shared memory; otherwise the word-mask layout, which reads the same tables through L1.
+// launch's shared memory; otherwise the same tables read through L1 (word masks, or pair tables).
 // Neither choice changes which candidates pass.
 uint32_t launch_layout(uint32_t layout, uint32_t words, uint32_t small_max, uint32_t nf_max,
                        const es_tune& tune, uint32_t stage_words) {
-    if (layout != ES_LAYOUT_SMEM) return layout;
+    if (layout != ES_LAYOUT_SMEM && layout != ES_LAYOUT_SMEM_PAIR) return layout;
+    const uint32_t fallback = layout == ES_LAYOUT_SMEM ? ES_LAYOUT_WORDMASK : ES_LAYOUT_PAIR;
     if (words != 1 && words != 2) return ES_LAYOUT_WORDMASK;
     const SmemPlan p = plan_smem(small_max, nf_max, tune, stage_words);
-    return p.bytes <= (uint32_t)g_dev.smem_optin - 1024u ? ES_LAYOUT_SMEM : ES_LAYOUT_WORDMASK;
+    return p.bytes <= (uint32_t)g_dev.smem_optin - 1024u ? layout : fallback;
 }
 
 // Filters of the inner-ring stage actually compiled into the launched kernel: word-mask kernels
@@ -234,6 +244,16 @@ uint64_t cycles_of(const EsInst& I, uint64_t ob, uint64_t oe, uint64_t* cb) {
     *cb = ob / I.r1;
     const uint64_t ce = (oe + I.r1 - 1) / I.r1;
     return ce - *cb;
+}
+
+// Warp-units of the ring-1 cycles [cb, ce) (the kernel's unit decode follows the same rule):
+// with a ring 2, 32 ring-2 rows x one window of at most `strip` ring-2 digits (ceil(r2 / strip)
+// balanced windows per row); without one, 32 lanes x `strip` consecutive cycles.
+uint64_t units_of(const EsInst& I, uint64_t cb, uint64_t ce, uint32_t strip) {
+    if (ce <= cb) return 0;
+    if (I.r2 <= 1) return (ce - cb + 32ull * strip - 1) / (32ull * strip);
+    const uint64_t rows = (ce + I.r2 - 1) / I.r2 - cb / I.r2;
+    return (rows + 31) / 32 * ((I.r2 + strip - 1) / strip);
 }
 
 }  // namespace
@@ -631,13 +651,13 @@ static int ctx_launch(es_ctx* c, uint64_t ob, uint64_t oe, const uint64_t* d_lis
     }
     const uint64_t per_unit = 32ull * tn.strip;
     it.unit_begin = 0;
-    it.n_units = (n_work + per_unit - 1) / per_unit;
+    it.n_units = d_list ? (n_work + per_unit - 1) / per_unit : units_of(I, it.c_begin, it.c_end, tn.strip);
     it.group = 0;
     it.inst_id = 0;
     const uint32_t F = stage_filters(tn.layout, tn.mask_filters, I.n_filters, I.F_built);
-    const uint32_t layout = launch_layout(tn.layout, I.W, I.small_bytes, I.n_filters, tn, I.mask_off[F]);
-    const SmemPlan sp = plan_smem((uint32_t)I.small_bytes, I.n_filters, tn,
-                                  layout == ES_LAYOUT_SMEM ? I.mask_off[F] : 0u);
+    const uint32_t layout = launch_layout(tn.layout, I.W, I.small_bytes, I.n_filters, tn,
+                                          stage_words_of(tn.layout, I, F));
+    const SmemPlan sp = plan_smem((uint32_t)I.small_bytes, I.n_filters, tn, stage_words_of(layout, I, F));
     it.caller = 0;
     L.items = nullptr;
     L.n_items = 1;
@@ -802,7 +822,6 @@ int es_batch_create(es_ctx* const* ctxs, uint32_t n_ctx, const es_batch_item* it
     b->ctxs.assign(ctxs, ctxs + n_ctx);
     for (uint32_t i = 0; i < n_ctx; ++i)
         if (!ctxs[i]) { es_batch_destroy(b); return fail(ES_ERR_ARG, "null context in batch"); }
-    const uint64_t per_unit = 32ull * tune.strip;
     // width class of a plan: the kernel instance its inner ring uses
     auto width_class = [](uint32_t W) -> uint32_t { return W <= 2 ? W : (W <= 4 ? 4u : 0u); };
     std::vector<uint32_t> h_tc;
@@ -829,7 +848,7 @@ int es_batch_create(es_ctx* const* ctxs, uint32_t n_ctx, const es_batch_item* it
         it.o_end = s.o_end;
         const uint64_t ncyc = s.o_end > s.o_begin ? cycles_of(I, s.o_begin, s.o_end, &it.c_begin) : 0;
         it.c_end = it.c_begin + ncyc;
-        it.n_units = (ncyc + per_unit - 1) / per_unit;
+        it.n_units = units_of(I, it.c_begin, it.c_end, tune.strip);
         it.group = s.group;
         it.inst_id = s.ctx_index;
         it.caller = i;
@@ -905,9 +924,10 @@ int es_batch_create(es_ctx* const* ctxs, uint32_t n_ctx, const es_batch_item* it
         sub.words = cls == 0 ? 0u : (cls == 4 && words == 0 ? 4u : (words ? words : cls));
         uint32_t stage_words = 0;   // the largest inner-stage tables among the class's plans
         for (uint32_t j = pos; j < end; ++j)
-            stage_words = std::max<uint32_t>(stage_words, ctxs[items[order[j]].ctx_index]->h_inst.mask_off[F]);
+            stage_words = std::max<uint32_t>(stage_words,
+                                             stage_words_of(tune.layout, ctxs[items[order[j]].ctx_index]->h_inst, F));
         sub.layout = launch_layout(tune.layout, sub.words, small_max, nf_max, tune, stage_words);
-        const SmemPlan sp = plan_smem(small_max, nf_max, tune, sub.layout == ES_LAYOUT_SMEM ? stage_words : 0u);
+        const SmemPlan sp = plan_smem(small_max, nf_max, tune, sub.layout == tune.layout ? stage_words : 0u);
         EsLaunch& L = sub.L;
         memset(&L, 0, sizeof(L));
         L.items = b->d_items_launch + pos;
@@ -1155,12 +1175,11 @@ extern "C" int es_search_blocks_static(const es_ctx* c, uint64_t t0, uint32_t n_
     const uint32_t F = stage_filters(tn.layout, tn.mask_filters, nf, I.F_built);
     es_tune tn0 = tn;
     tn0.count_stages = 0;   // the static search never counts
-    const uint32_t layout = launch_layout(tn.layout, I.W, I.small_bytes, nf, tn0, I.mask_off[F]);
-    const SmemPlan sp = plan_smem((uint32_t)I.small_bytes, nf, tn0, layout == ES_LAYOUT_SMEM ? I.mask_off[F] : 0u);
-    const uint64_t per_unit = 32ull * tn.strip;
+    const uint32_t layout = launch_layout(tn.layout, I.W, I.small_bytes, nf, tn0, stage_words_of(tn.layout, I, F));
+    const SmemPlan sp = plan_smem((uint32_t)I.small_bytes, nf, tn0, stage_words_of(layout, I, F));
     uint64_t cbeg = 0;
     const uint64_t ncyc = cycles_of(I, 0, I.n_outer, &cbeg);
-    const uint64_t nu = (ncyc + per_unit - 1) / per_unit;
+    const uint64_t nu = units_of(I, cbeg, cbeg + ncyc, tn.strip);
     for (uint32_t i = 0; i < n_blocks; ++i) {
         const uint64_t t = t0 + i;
         EsItem& it = g_static_items[i];

@@ -91,7 +91,7 @@ struct EsLaunch {
     uint32_t threads;
     uint32_t strip;
     uint32_t mask_filters;   // F requested (template F is the rounded-up instance)
-    uint64_t total_units;          // warp-units: 32 lanes x strip ring-1 cycles (or list entries)
+    uint64_t total_units;          // warp-units: 32 lanes x <= strip ring-1 cycles (or list entries)
     uint32_t nf_max;               // largest filter count among the launch's plans
     uint32_t direct;               // 1: every item uses one plan (no CTA barriers after staging)
     unsigned long long* unit_counter;     // single-plan launches: next warp-unit
@@ -103,20 +103,21 @@ struct EsLaunch {
     uint32_t smem_bytes;              // dynamic shared memory of the launch
     uint32_t cnt_off;                 // byte offset of the per-warp tail-stage counters in smem
     uint32_t queue_off;               // byte offset of the per-warp survivor queues in smem
-    uint32_t stage_off;               // byte offset of the staged phase tables (ES_LAYOUT_SMEM)
+    uint32_t stage_off;               // byte offset of the staged tables (ES_LAYOUT_SMEM, _SMEM_PAIR)
     // single-plan launches carry their one item and block constants by value
     EsItem item0;
     uint32_t tconst0[ES_MAX_FILTERS];
 };
 
 // Scan kernel instances by layout (es_scan_wm.cu / es_scan_wmc.cu, es_scan_pair.cu, es_scan_sc.cu,
-// es_scan_sm.cu).
+// es_scan_sm.cu, es_scan_sp.cu).
 typedef void (*ScanFn)(const EsLaunch);
 ScanFn es_pick_wordmask_fast(uint32_t words, uint32_t mask_filters);
 ScanFn es_pick_wordmask_count(uint32_t words, uint32_t mask_filters);
 ScanFn es_pick_pair(int count, uint32_t words, uint32_t mask_filters);
 ScanFn es_pick_scalar(int count, uint32_t mask_filters);
 ScanFn es_pick_smem(int count, uint32_t words, uint32_t mask_filters);
+ScanFn es_pick_smem_pair(int count, uint32_t words, uint32_t mask_filters);
 
 // Host-side launchers implemented in es_scan.cu (return a cudaError_t value).
 int es_scan_prepare(int smem_optin_bytes);

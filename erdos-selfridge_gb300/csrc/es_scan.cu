@@ -1,8 +1,8 @@
 // Dispatch of the scan kernel instances, the block-ordered min-reduction and the integer-pipe
 // peak probe of the GB300 Erdős–Selfridge CRT-wheel sieve (sm_103a).  The scan kernel itself is
 // es_scan_kernel.cuh, instantiated per layout in es_scan_wm.cu / es_scan_wmc.cu (word masks,
-// production and counting launches), es_scan_pair.cu, es_scan_sc.cu and es_scan_sm.cu (word masks
-// staged in shared memory).
+// production and counting launches), es_scan_pair.cu, es_scan_sc.cu, es_scan_sm.cu (word masks
+// staged in shared memory) and es_scan_sp.cu (pair tables staged in shared memory).
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -128,6 +128,7 @@ ScanFn pick(int layout, int count, uint32_t words, uint32_t f) {
     // staged tables exist for inner rings of one or two words (the host resolves any other
     // ring to the word-mask layout before it asks)
     if (layout == ES_LAYOUT_SMEM) return (words == 1 || words == 2) ? es_pick_smem(count, words, f) : nullptr;
+    if (layout == ES_LAYOUT_SMEM_PAIR) return (words == 1 || words == 2) ? es_pick_smem_pair(count, words, f) : nullptr;
     // pair tables exist for inner rings of one or two words.  words == 0 (a batch whose plans
     // differ in width) and wider rings take the generic word-mask instance, which reads each
     // plan's own width: a fixed-width instance would index past a narrower plan's tables.
@@ -141,11 +142,11 @@ ScanFn pick(int layout, int count, uint32_t words, uint32_t f) {
 int es_scan_prepare(int smem_optin_bytes) {
     const uint32_t fs[8] = {0, 1, 2, 3, 4, 5, 6, 8};
     const uint32_t ws[4] = {1, 2, 3, 5};   // every word-count instance: 1, 2, 3-4, generic
-    for (int layout = 0; layout < 4; ++layout)
+    for (int layout = 0; layout < 5; ++layout)
         for (int count = 0; count < 2; ++count)
             for (uint32_t w : ws)
                 for (uint32_t f : fs) {
-                    if (layout == ES_LAYOUT_SMEM && w > 2) continue;
+                    if ((layout == ES_LAYOUT_SMEM || layout == ES_LAYOUT_SMEM_PAIR) && w > 2) continue;
                     const ScanFn fn = pick(layout, count, w, f);
                     if (!fn) return (int)cudaErrorInvalidDeviceFunction;
                     cudaError_t e = cudaFuncSetAttribute(fn,

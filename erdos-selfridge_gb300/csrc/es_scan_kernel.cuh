@@ -17,7 +17,10 @@
 //    search).
 //  * Two-level strip mining.  A lane owns `strip` consecutive ring-1 cycles (cycle index =
 //    oidx / r1).  Rings >= 2 give b2 = sum term_j mod M, decoded once per strip and then
-//    stepped with a 128-bit delta table when the ring-2 digit advances.  Ring 1 is swept in a
+//    stepped with a 128-bit delta table when the ring-2 digit advances.  The 32 lanes of a warp
+//    take 32 consecutive ring-2 rows over the same window of ring-2 digits, so the per-step
+//    delta rows are broadcast loads (lanes on different digits of a 21-digit ring 2 read up to
+//    21 rows of a 32-byte stride: a 6-way bank conflict per load).  Ring 1 is swept in a
 //    warp-uniform loop (b = b2 + T1[d1], broadcast loads) and ring 0, the inner ring, is
 //    handled 32 candidates at a time as bit masks.
 //  * 128-bit values are four 32-bit limbs with PTX carry chains; filter residues are carried
@@ -126,6 +129,11 @@ __device__ __forceinline__ uint2 lds64(uint32_t saddr) {
     asm("ld.shared.v2.u32 {%0, %1}, [%2];" : "=r"(v.x), "=r"(v.y) : "r"(saddr));
     return v;
 }
+__device__ __forceinline__ uint4 lds128(uint32_t saddr) {
+    uint4 v;
+    asm("ld.shared.v4.u32 {%0, %1, %2, %3}, [%4];" : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "r"(saddr));
+    return v;
+}
 
 // Volatile shared loads: values the ring-1 sweep needs only on its rare paths are re-read where
 // they are used instead of being held in registers across the sweep.
@@ -199,7 +207,8 @@ struct TailCtx {
     unsigned long long* surv_n;
     unsigned long long* group_found;
     uint64_t surv_cap;
-    uint32_t kp1, Feff, FR, nf, wcnt_saddr, item_id, group, r0, r1, strip;
+    uint32_t kp1, Feff, FR, nf, wcnt_saddr, item_id, group, r0, r1;
+    uint32_t lstride;                  // entries between the strips of consecutive lanes
     bool M_big;
 };
 
@@ -215,7 +224,8 @@ struct TailCtx {
 #define ES_NRES 4
 struct EsQueue {
     uint4 ent[ES_QCAP];
-    uint4 rec[32][2];                  // per lane: b2 (limbs); residues of b2 + block term
+    uint4 rec0[32];                    // per lane: b2 (limbs)
+    uint4 rec1[32];                    // per lane: residues of b2 + block term (residue stage)
     TailCtx ctx;                       // the warp's current item (see TailCtx)
 };
 static_assert(sizeof(EsQueue) <= ES_QUEUE_BYTES, "per-warp slot overflows its shared-memory share");
@@ -313,7 +323,9 @@ __device__ __forceinline__ void flush(EsQueue* Q, const unsigned char* smem, con
     const uint32_t own = has ? (en.w & 31u) : 0u;
     const bool wrap1 = has && ((en.w >> 5) & 1u);
     const bool cw = has && slot >= (en.z >> 16);   // sorted slots from the split on wrap past M
-    const uint4 bq = Q->rec[own][1];
+    // lanes without an entry run the residue stage's loads too: give them zero residues, not
+    // another lane's record (lane 0 of a unit may not have reached its first cycle yet)
+    const uint4 bq = has ? Q->rec1[own] : make_uint4(0u, 0u, 0u, 0u);
     const uint32_t bqv[ES_NRES] = {bq.x, bq.y, bq.z, bq.w};
     const uint32_t f0 = C.Feff, fr = C.FR, r0 = C.r0;
     bool ok = has;
@@ -333,9 +345,9 @@ __device__ __forceinline__ void flush(EsQueue* Q, const unsigned char* smem, con
     }
     if (ok) {
         uint32_t wm;
-        const U4 b = addmod(u4(Q->rec[own][0]), u4(sT1[d1]), C.M, wm);
+        const U4 b = addmod(u4(Q->rec0[own]), u4(sT1[d1]), C.M, wm);
         const U4 s = addmod(b, u4(sS0[slot]), C.M, wm);
-        const uint64_t e = C.e_base + (uint64_t)own * C.strip + step;
+        const uint64_t e = C.e_base + (uint64_t)own * C.lstride + step;
         const uint64_t oidx = C.list ? __ldg(C.list + e) : e * C.r1 + d1;
         tail_one<COUNT>(C, sFC, fr, s, oidx * (uint64_t)r0 + sI0[slot]);
     }
@@ -393,6 +405,32 @@ __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, u
     }
     // residue stage: the next ES_NRES filters that carry 32-bit term residues
     const uint32_t FR = min(si.F_built, Feff + ES_NRES) > Feff ? min(si.F_built, Feff + ES_NRES) : Feff;
+    // This unit's entries.  Ranges with a ring 2: unit u is ring-2 rows row0 + 32*(u / J) + lane
+    // (lane by lane) over the digit window [j*r2/J, (j+1)*r2/J), j = u mod J, J = ceil(r2 /
+    // strip) (J windows of at most `strip` digits, balanced); cycles outside [c_begin, c_end) are
+    // skipped.  Lists, and ranges without a ring 2: `strip` consecutive entries per lane, lane
+    // after lane.
+    const uint64_t u = w - item.unit_begin;
+    uint64_t e_base, e_lo, e_min, e_hi;
+    uint32_t lstride, nsteps;
+    if (!list && r2 > 1u) {
+        const uint32_t J = (r2 + L.strip - 1u) / L.strip;
+        const uint64_t rb = u / J;
+        const uint32_t j = (uint32_t)(u - rb * J);
+        const uint32_t wlo = j * r2 / J;
+        nsteps = (j + 1u) * r2 / J - wlo;
+        lstride = r2;
+        e_base = (item.c_begin / r2 + rb * 32ull) * r2 + wlo;
+        e_lo = e_base + (uint64_t)lane * r2;
+        e_min = max(e_lo, item.c_begin);
+        e_hi = min(e_lo + nsteps, item.c_end);
+    } else {
+        nsteps = L.strip;
+        lstride = L.strip;
+        e_base = (list ? ob : item.c_begin) + u * 32ull * L.strip;
+        e_lo = e_min = e_base + (uint64_t)lane * L.strip;
+        e_hi = min(e_lo + L.strip, list ? oe : item.c_end);
+    }
     TailCtx& C = Q->ctx;
     if (lane == 0) {
         C.M = M;
@@ -414,59 +452,50 @@ __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, u
         C.Feff = Feff;
         C.FR = FR;
         C.r1 = si.r1;
-        C.strip = L.strip;
+        C.lstride = lstride;
         C.list = reinterpret_cast<const unsigned long long*>(item.list);
-        C.e_base = (item.list ? item.o_begin : item.c_begin) + (w - item.unit_begin) * 32ull * L.strip;
+        C.e_base = e_base;
     }
     __syncwarp();
     constexpr int FA = F > 0 ? F : 1;   // array extent
     // word-mask phase tables, in global memory or staged in shared memory by the launch
     constexpr bool WMASK = LAYOUT == ES_LAYOUT_WORDMASK || LAYOUT == ES_LAYOUT_SMEM;
+    constexpr bool PAIRL = LAYOUT == ES_LAYOUT_PAIR || LAYOUT == ES_LAYOUT_SMEM_PAIR;
     uint32_t qf[FA], corr[FA];
     const uint32_t* tab[FA];
-    uint32_t tabs[FA];   // shared address of each staged table (ES_LAYOUT_SMEM)
+    uint32_t tabs[FA];   // shared address of each staged table (ES_LAYOUT_SMEM, ES_LAYOUT_SMEM_PAIR)
 #pragma unroll
     for (int f = 0; f < F; ++f) {
         const bool on = (uint32_t)f < Feff;
         qf[f] = on ? sFC[f].q : 1u;
         corr[f] = on ? sFC[f].corr : 0u;
         tab[f] = LAYOUT == ES_LAYOUT_WORDMASK ? masks_g + si.mask_off[f]
-                 : LAYOUT == ES_LAYOUT_PAIR   ? si.pairs + 2u * si.mask_off[f]
+                 : PAIRL                      ? si.pairs + 2u * si.mask_off[f]
                                               : si.allowed + (on ? sFC[f].off : 0u);
-        tabs[f] = (uint32_t)__cvta_generic_to_shared(smem + L.stage_off) + 4u * si.mask_off[f];
+        tabs[f] = (uint32_t)__cvta_generic_to_shared(smem + L.stage_off) +
+                  4u * (LAYOUT == ES_LAYOUT_SMEM_PAIR ? 2u : 1u) * si.mask_off[f];
     }
     uint32_t cnt[FA];
 #pragma unroll
     for (int f = 0; f < FA; ++f) cnt[f] = 0u;
     uint32_t qhead = 0, qsize = 0;
 
-    const uint64_t rel = (w - item.unit_begin) * 32ull * L.strip + (uint64_t)lane * L.strip;
-    uint64_t e_lo, e_hi;
-    if (list) {
-        e_lo = ob + rel;
-        e_hi = e_lo + L.strip;
-        if (e_hi > oe) e_hi = oe;
-    } else {
-        e_lo = item.c_begin + rel;
-        e_hi = e_lo + L.strip;
-        if (e_hi > item.c_end) e_hi = item.c_end;
-    }
     uint32_t d2 = 0;
     uint32_t BQ2[FA];
 #pragma unroll
     for (int f = 0; f < FA; ++f) BQ2[f] = 0u;
     bool have = false;
     uint64_t prev_c = 0;
-    // every lane runs L.strip steps so the warp-wide votes below see 32 lanes
-    for (uint32_t step = 0; step < L.strip; ++step) {
+    // every lane runs the unit's steps so the warp-wide votes below see 32 lanes
+    for (uint32_t step = 0; step < nsteps; ++step) {
         const uint64_t e = e_lo + step;
-        const bool live = e < e_hi;
-        if (__ballot_sync(0xffffffffu, live) == 0u) break;
+        const bool live = e >= e_min && e < e_hi;
+        if (__ballot_sync(0xffffffffu, e < e_hi) == 0u) break;   // no lane has entries left
         uint64_t c = prev_c;
         uint32_t lo1 = 0u, hi1 = 0u;
         // b2 of the lane's last cycle lives in its record (0 before the first decode)
         const U4 Mv = ldv_M(si);
-        U4 b2 = have ? ldv128(&Q->rec[lane][0]) : U4{0u, 0u, 0u, 0u};
+        U4 b2 = have ? ldv128(&Q->rec0[lane]) : U4{0u, 0u, 0u, 0u};
         if (live) {
             if (list) {
                 const uint64_t o = __ldg(reinterpret_cast<const unsigned long long*>(list) + e);
@@ -489,15 +518,15 @@ __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, u
 #pragma unroll
                 for (int f = 0; f < F; ++f) BQ2[f] = red2(BQ2[f] + dq[f] + (corr[f] & wm), qf[f]);
                 // this lane's record: b2 and the residue-stage residues, stepped the same way
-                const uint4 rq = Q->rec[lane][1];
+                const uint4 rq = Q->rec1[lane];
                 uint32_t rv[ES_NRES] = {rq.x, rq.y, rq.z, rq.w};
 #pragma unroll
                 for (uint32_t j = 0; j < ES_NRES; ++j) {
                     const uint32_t f = Feff + j;
                     if (f < FR) rv[j] = red2(rv[j] + sDQ2w[d2 * ES_FMAX + f] + (sFC[f].corr & wm), sFC[f].q);
                 }
-                Q->rec[lane][0] = make_uint4(b2.x, b2.y, b2.z, b2.w);
-                Q->rec[lane][1] = make_uint4(rv[0], rv[1], rv[2], rv[3]);
+                Q->rec0[lane] = make_uint4(b2.x, b2.y, b2.z, b2.w);
+                Q->rec1[lane] = make_uint4(rv[0], rv[1], rv[2], rv[3]);
                 ++d2;
             } else if (!(have && c == prev_c)) {
                 b2 = decode_cycle(si, c, Mv, d2);
@@ -511,12 +540,16 @@ __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, u
                     const uint32_t f = Feff + j;
                     if (f < FR) rv[j] = red1(mod128(b2, sFC[f]) + tcv[f], sFC[f].q);
                 }
-                Q->rec[lane][0] = make_uint4(b2.x, b2.y, b2.z, b2.w);
-                Q->rec[lane][1] = make_uint4(rv[0], rv[1], rv[2], rv[3]);
+                Q->rec0[lane] = make_uint4(b2.x, b2.y, b2.z, b2.w);
+                Q->rec1[lane] = make_uint4(rv[0], rv[1], rv[2], rv[3]);
                 have = true;
             }
             prev_c = c;
         }
+        // the inner-stage residues with the ring-1 wrap correction added, once per cycle
+        uint32_t BQ2c[FA];
+#pragma unroll
+        for (int f = 0; f < FA; ++f) BQ2c[f] = red1(BQ2[f] + corr[f], qf[f]);
         // A = M - b2 and its 32-bit key, once per ring-1 cycle
         uint32_t brA;
         const uint32_t KA = key32(sub128(Mv, b2, brA), ldv32(&si.sh));
@@ -532,7 +565,7 @@ __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, u
             // carry split of the inner ring: slots [split, r0) wrap past M.  Away from a key tie,
             // t is the key of thr = M - b to within +-1 and fits 32 bits (0 <= t <= KM); keys
             // below t-1 are certainly below thr, keys above t+1 certainly not.
-            const uint32_t t = wm1 ? KM - (k1 - KA) : KA - k1;
+            const uint32_t t = KA - k1 + (KM & wm1);          // KM - (k1 - KA) on a wrap
             const uint32_t tl = max(t, 1u) - 1u;
             const uint32_t th = min(t, 0xfffffffeu) + 1u;
             // the bucket of tl holds its first slot and the next three keys (sorted): the split
@@ -548,7 +581,7 @@ __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, u
                 if (rare) {
                     uint32_t wx, brw;
                     const U4 Mr = ldv_M(si);
-                    const U4 b = addmod(ldv128(&Q->rec[lane][0]), ldv128(smem + ldv32(&si.o_T1) + 16u * d1), Mr, wx);
+                    const U4 b = addmod(ldv128(&Q->rec0[lane]), ldv128(smem + ldv32(&si.o_T1) + 16u * d1), Mr, wx);
                     wm1 = wx;
                     const U4 thr = sub128(Mr, b, brw);
                     const uint32_t te = key32(thr, ldv32(&si.sh));
@@ -560,7 +593,7 @@ __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, u
                 }
             }
 
-            if (LAYOUT == ES_LAYOUT_PAIR) {
+            if (PAIRL) {
                 // pair tables: the row of phase x0 holds the masks for both sides of the carry
                 // split, so a filter costs one load (8 B for one word, 16 B for two)
                 uint32_t b0 = act ? (WT == 1 ? tail : 0xffffffffu) : 0u, b1 = act && WT == 2 ? tail : 0u;
@@ -568,12 +601,14 @@ __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, u
                 const uint32_t cm1 = __funnelshift_lc(0u, 0xffffffffu, max(split, 32u) - 32u) & tail;
 #pragma unroll
                 for (int f = 0; f < F; ++f) {
-                    const uint32_t x0 = red2(BQ2[f] + tq[f] + (corr[f] & wm1), qf[f]);
+                    const uint32_t x0 = red1((wm1 ? BQ2c[f] : BQ2[f]) + tq[f], qf[f]);
                     if (WT == 1) {
-                        const uint2 m = __ldg(reinterpret_cast<const uint2*>(tab[f]) + x0);
+                        const uint2 m = LAYOUT == ES_LAYOUT_SMEM_PAIR ? lds64(tabs[f] + 8u * x0)
+                                                                      : __ldg(reinterpret_cast<const uint2*>(tab[f]) + x0);
                         b0 &= (m.x & ~cm0) | (m.y & cm0);
                     } else {
-                        const uint4 m = __ldg(reinterpret_cast<const uint4*>(tab[f]) + x0);
+                        const uint4 m = LAYOUT == ES_LAYOUT_SMEM_PAIR ? lds128(tabs[f] + 16u * x0)
+                                                                      : __ldg(reinterpret_cast<const uint4*>(tab[f]) + x0);
                         b0 &= (m.x & ~cm0) | (m.z & cm0);
                         b1 &= (m.y & ~cm1) | (m.w & cm1);
                     }
@@ -595,7 +630,7 @@ __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, u
                 }
 #pragma unroll
                 for (int f = 0; f < F; ++f) {
-                    const uint32_t x0 = red2(BQ2[f] + tq[f] + (corr[f] & wm1), qf[f]);
+                    const uint32_t x0 = red1((wm1 ? BQ2c[f] : BQ2[f]) + tq[f], qf[f]);
                     const uint32_t x1 = red1(x0 + corr[f], qf[f]);
                     const uint4 m0 = __ldg(reinterpret_cast<const uint4*>(tab[f]) + x0);
                     const uint4 m1 = __ldg(reinterpret_cast<const uint4*>(tab[f]) + x1);
@@ -619,7 +654,7 @@ __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, u
                 const uint32_t cm1 = __funnelshift_lc(0u, 0xffffffffu, max(split, 32u) - 32u) & tail;
 #pragma unroll
                 for (int f = 0; f < F; ++f) {
-                    const uint32_t x0 = red2(BQ2[f] + tq[f] + (corr[f] & wm1), qf[f]);
+                    const uint32_t x0 = red1((wm1 ? BQ2c[f] : BQ2[f]) + tq[f], qf[f]);
                     const uint32_t x1 = red1(x0 + corr[f], qf[f]);
                     const uint2 m0 = LAYOUT == ES_LAYOUT_SMEM ? lds64(tabs[f] + 8u * x0)
                                                               : __ldg(reinterpret_cast<const uint2*>(tab[f]) + x0);
@@ -644,7 +679,7 @@ __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, u
                     // straight-line cascade: two table loads per filter per 32 candidates
 #pragma unroll
                     for (int f = 0; f < F; ++f) {
-                        const uint32_t x0 = red2(BQ2[f] + tq[f] + (corr[f] & wm1), qf[f]);   // n mod q_f, ring-0 base
+                        const uint32_t x0 = red1((wm1 ? BQ2c[f] : BQ2[f]) + tq[f], qf[f]);   // n mod q_f, ring-0 base
                         const uint32_t x1 = red1(x0 + corr[f], qf[f]);                      // the same after a wrap
                         const uint32_t m0 = LAYOUT == ES_LAYOUT_SMEM ? lds32(tabs[f] + 4u * (x0 * RSn + wd))
                                                                      : __ldg(tab[f] + x0 * RSn + wd);
@@ -658,7 +693,7 @@ __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, u
 #pragma unroll
                     for (int f = 0; f < F; ++f) {
                         if (alive && (uint32_t)f < Feff) {
-                            const uint32_t bqf = red2(BQ2[f] + tq[f] + (corr[f] & wm1), qf[f]);
+                            const uint32_t bqf = red1((wm1 ? BQ2c[f] : BQ2[f]) + tq[f], qf[f]);
                             uint32_t nb = 0u, live_bits = bits;
                             while (live_bits) {
                                 const uint32_t i = __ffs(live_bits) - 1u;
@@ -708,8 +743,8 @@ __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, u
     }
 }
 
-// Work distribution.  A warp-unit is 32 lanes x `strip` consecutive ring-1 cycles (or list
-// entries) of one item.  Single-plan launches: the CTA stages the plan's tables once, then each
+// Work distribution.  A warp-unit is 32 lanes x up to `strip` ring-1 cycles (or list entries)
+// of one item (lanes on consecutive ring-2 rows, see scan_unit).  Single-plan launches: the CTA stages the plan's tables once, then each
 // warp claims warp-units from the global counter on its own -- no CTA barrier after staging.
 // Several plans: a CTA works on one item at a time, its warps claim the item's warp-units from
 // the item's own counter, and the CTA synchronises only when it moves to another item (and
@@ -744,6 +779,8 @@ __global__ void __launch_bounds__(ES_LB_THREADS, ES_LB_MINB) es_scan_kernel(cons
         copy_words(reinterpret_cast<uint32_t*>(smem), reinterpret_cast<const uint32_t*>(si.small), si.small_bytes >> 2);
         if (LAYOUT == ES_LAYOUT_SMEM)   // the inner-stage filters' phase tables (16-byte aligned)
             copy_words(reinterpret_cast<uint32_t*>(smem + L.stage_off), si.masks, si.mask_off[F]);
+        if (LAYOUT == ES_LAYOUT_SMEM_PAIR)
+            copy_words(reinterpret_cast<uint32_t*>(smem + L.stage_off), si.pairs, 2u * si.mask_off[F]);
         __syncthreads();
         for (;;) {
             unsigned long long w = 0;
@@ -802,6 +839,8 @@ __global__ void __launch_bounds__(ES_LB_THREADS, ES_LB_MINB) es_scan_kernel(cons
                        si.small_bytes >> 2);
             if (LAYOUT == ES_LAYOUT_SMEM)
                 copy_words(reinterpret_cast<uint32_t*>(smem + L.stage_off), si.masks, si.mask_off[F]);
+            if (LAYOUT == ES_LAYOUT_SMEM_PAIR)
+                copy_words(reinterpret_cast<uint32_t*>(smem + L.stage_off), si.pairs, 2u * si.mask_off[F]);
             __syncthreads();
             cur_inst = item.inst_id;
         }

@@ -1,8 +1,9 @@
 """Autotuner for the scan kernel's launch shape and table layout.
 
-Chooses, per plan (or per batch), the fastest of: threads per CTA, strip depth (ring-1 cycles
-per lane per work unit, i.e. residues per thread per unit = strip * r1 * r0), the table layout
-(word-mask vs scalar) and the number of filters evaluated in the inner-ring stage.  None of
+Chooses, per plan (or per batch), the fastest of: threads per CTA, strip depth (at most `strip`
+ring-1 cycles per lane per work unit: one balanced window of ring-2 digits), the table layout
+(word masks or pair tables, through L1 or staged in shared memory, or scalar) and the number of
+filters evaluated in the inner-ring stage.  None of
 these changes which candidates pass; the tuner only times.  Search: coordinate descent from the
 default shape over one parameter at a time, each candidate timed with CUDA events on a probe
 range (median of a few launches).  Results are cached in a JSON file keyed by the plan (k,
@@ -20,11 +21,11 @@ import es_native as N
 
 SPACE = {
     "threads": [256, 384, 512],
-    "strip": [1, 2, 4],
+    "strip": [2, 4, 8, 16],
     "mask_filters": [2, 3, 4, 5, 6],
-    "layout": [N.LAYOUT_WORDMASK, N.LAYOUT_PAIR, N.LAYOUT_SMEM, N.LAYOUT_SCALAR],
+    "layout": [N.LAYOUT_WORDMASK, N.LAYOUT_PAIR, N.LAYOUT_SMEM, N.LAYOUT_SMEM_PAIR, N.LAYOUT_SCALAR],
 }
-DEFAULT = dict(layout=N.LAYOUT_WORDMASK, mask_filters=4, threads=512, strip=2, smem_kb=0,
+DEFAULT = dict(layout=N.LAYOUT_WORDMASK, mask_filters=4, threads=512, strip=8, smem_kb=0,
                ctas_per_sm=4, count_stages=0)
 
 

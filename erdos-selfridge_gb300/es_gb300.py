@@ -50,7 +50,7 @@ TUNABLES.update({
     "chunk_log2": 34,        # positions per _launch chunk issued by scan_block
     "layout": "auto",        # "auto" (by table bytes) | "wordmask" | "pair" | "smem" | "scalar"
     "threads": 512,          # CTA size
-    "strip": 2,              # ring-1 cycles per lane per warp-unit
+    "strip": 8,              # at most this many ring-1 cycles per lane per warp-unit
     "smem_kb": 0,            # accepted, no effect (phase tables are read through L1)
     "ctas_per_sm": 4,
     "count_stages": 0,       # per-filter-stage pass counts (es_stage_counts needs 1)
@@ -74,9 +74,10 @@ def _tune_from(tun: dict, plan=None) -> N.Tune:
     if layout == "auto":
         code = N.layout_for_plan(plan, F) if plan is not None else N.LAYOUT_WORDMASK
     else:
-        code = {"scalar": N.LAYOUT_SCALAR, "pair": N.LAYOUT_PAIR, "smem": N.LAYOUT_SMEM}.get(layout, N.LAYOUT_WORDMASK)
+        code = {"scalar": N.LAYOUT_SCALAR, "pair": N.LAYOUT_PAIR, "smem": N.LAYOUT_SMEM,
+                "smem-pair": N.LAYOUT_SMEM_PAIR}.get(layout, N.LAYOUT_WORDMASK)
     return N.make_tune(layout=code, mask_filters=F,
-                       threads=int(tun.get("threads", 512)), strip=int(tun.get("strip", 2)),
+                       threads=int(tun.get("threads", 512)), strip=int(tun.get("strip", 8)),
                        smem_kb=int(tun.get("smem_kb", 0)), ctas_per_sm=int(tun.get("ctas_per_sm", 4)),
                        count_stages=int(tun.get("count_stages", 0)))
 
@@ -201,7 +202,8 @@ class GpuSieve:
         self.launches = 0
         self.residues_checked = 0
         self.mask_mode = {N.LAYOUT_SCALAR: "scalar-gb300", N.LAYOUT_PAIR: "pair-gb300",
-                          N.LAYOUT_SMEM: "smem-gb300"}.get(self.tune.layout, "wordmask-gb300")
+                          N.LAYOUT_SMEM: "smem-gb300", N.LAYOUT_SMEM_PAIR: "smem-pair-gb300"}.get(
+            self.tune.layout, "wordmask-gb300")
         self.tconst = _Tconst(self)
         self.out_n = _OutN(self)
         self.out = _Out(self)

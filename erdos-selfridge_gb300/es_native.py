@@ -21,6 +21,7 @@ LAYOUT_WORDMASK = 0
 LAYOUT_SCALAR = 1
 LAYOUT_PAIR = 2       # word masks with the wrapped row beside each phase (inner rings <= 64 slots)
 LAYOUT_SMEM = 3       # word masks of the inner-stage filters staged in shared memory (<= 64 slots)
+LAYOUT_SMEM_PAIR = 4  # pair tables of the inner-stage filters staged in shared memory (<= 64 slots)
 MAX_MASK_FILTERS = 8
 
 
@@ -211,7 +212,7 @@ def layout_for_plan(plan, mask_filters: int) -> int:
     return layout_for(plan.radix[0] if plan.radix else 1, [plan.info[p][0] for p in plan.rest], mask_filters)
 
 
-def make_tune(layout=LAYOUT_WORDMASK, mask_filters=4, threads=512, strip=2, smem_kb=0,
+def make_tune(layout=LAYOUT_WORDMASK, mask_filters=4, threads=512, strip=8, smem_kb=0,
               ctas_per_sm=4, count_stages=1) -> Tune:
     return Tune(layout=int(layout), mask_filters=int(mask_filters), threads=int(threads),
                 strip=int(strip), smem_kb=int(smem_kb), ctas_per_sm=int(ctas_per_sm),

@@ -24,6 +24,10 @@ SHAPES = [
     dict(layout=2, mask_filters=3, threads=512, strip=5),
     dict(layout=3, mask_filters=4, threads=512, strip=2),
     dict(layout=3, mask_filters=6, threads=256, strip=3),
+    dict(layout=4, mask_filters=4, threads=512, strip=2),
+    dict(layout=4, mask_filters=5, threads=256, strip=3),
+    dict(layout=3, mask_filters=4, threads=512, strip=8),
+    dict(layout=0, mask_filters=3, threads=256, strip=64),   # windows wider than ring 2
 ]
 
 
@@ -70,7 +74,8 @@ def test_k300_seeded_sample(native):
     plan = es_gb300.Plan(300)
     assert [[p, T] for p, T in plan.wheel] == g["plan"]["wheel"]
     outer = _sample(g["seed"], g["domain"], g["draws"], g["outer_sha256"])
-    for shape in (SHAPES[0], SHAPES[3], SHAPES[5], SHAPES[7], dict(layout=0, mask_filters=8, threads=512, strip=16)):
+    for shape in (SHAPES[0], SHAPES[3], SHAPES[5], SHAPES[7], SHAPES[9],
+                  dict(layout=0, mask_filters=8, threads=512, strip=16)):
         ctx = N.Context(plan, _tune(N, **shape))
         ctx.set_block(0)
         ctx.reset()
@@ -91,7 +96,7 @@ def test_k390_seeded_sample(native, role):
     assert str(plan.M) == g["plan"]["M"] and plan.rest == g["plan"]["rest"]
     outer = _sample(g["seed"], g["domain"], g["draws"], g["outer_sha256"])
     for shape in (dict(mask_filters=8), dict(layout=2, mask_filters=4), dict(layout=2, mask_filters=3, strip=1),
-                  dict(layout=3, mask_filters=2)):
+                  dict(layout=3, mask_filters=2), dict(layout=4, mask_filters=3)):
         ctx = N.Context(plan, _tune(N, **shape))
         ctx.set_block(0)
         ctx.reset()
@@ -289,17 +294,25 @@ def test_min_survivor_and_overflow(native):
 
 
 def test_edge_ranges(native):
-    """Empty ranges, ranges inside one ring-1 cycle, duplicates in a list, range checks."""
+    """Empty ranges, ranges inside one ring-1 cycle, ranges that start and end inside a ring-2
+    row (a warp-unit spans 32 rows, so its first lanes may start later than the rest),
+    duplicates in a list, range checks."""
     import es_gb300
     import es_oracle as O
     N = native
     plan = es_gb300.Plan(200)
+    r1, r2 = plan.radix[1], plan.radix[2]
+    row = r1 * r2   # outer indices per ring-2 row
+    ranges = ((0, 0), (5, 6), (r1 - 1, r1 + 1), (3 * r1 + 2, 7 * r1 + 5), (row - 1, row + 1),
+              (5 * row + 3 * r1 + 1, 40 * row + 7), (2 * row, 70 * row), (33 * row - 5, 33 * row + r1 * 3))
+    for strip in (4, 64):
+        ctx = N.Context(plan, _tune(N, strip=strip))
+        for ob, oe in ranges + ((ctx.n_outer - 3, ctx.n_outer),):
+            s, c = _scan(N, ctx, 2, ob, oe)
+            ws, wc, _ = O.scan_c(plan, 2, o_range=(ob, oe))
+            assert s == ws and c == wc, (strip, ob, oe)
+        ctx.close()
     ctx = N.Context(plan, _tune(N))
-    r1 = plan.radix[1]
-    for ob, oe in ((0, 0), (5, 6), (r1 - 1, r1 + 1), (3 * r1 + 2, 7 * r1 + 5), (ctx.n_outer - 3, ctx.n_outer)):
-        s, c = _scan(N, ctx, 2, ob, oe)
-        ws, wc, _ = O.scan_c(plan, 2, o_range=(ob, oe))
-        assert s == ws and c == wc, (ob, oe)
     lst = np.array([9, 9, 1, 12345, 9], dtype=np.uint64)
     ctx.set_block(1)
     ctx.reset()
