@@ -268,6 +268,8 @@ def main():
     ap.add_argument("--bfile", default=None)
     ap.add_argument("--log2-positions", type=int, default=40)
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--tune", type=json.loads, default=None,
+                    help="k390: launch shape (JSON, es_autotune.DEFAULT keys) instead of the default")
     a = ap.parse_args()
     if a.which == "small-k":
         known = {k: g for k, (g, _) in es_gb300.load_known(a.bfile).items()} if a.bfile else None
@@ -275,7 +277,13 @@ def main():
     elif a.which == "batch64":
         out = batch64(autotune=not a.no_autotune)
     elif a.which == "k390":
-        out = k390(a.log2_positions)
+        orders = None
+        if a.model:   # the learned planner's cascade order for each wheel
+            import es_learned
+            model = es_learned.CostModel.load(a.model)
+            orders = {role: es_learned.learned_order(model, es_gb300.Plan(390, None, w))[1]
+                      for role, w in K390_WHEELS.items()}
+        out = k390(a.log2_positions, filter_orders=orders, tune=a.tune)
     elif a.which == "mitm":
         out = mitm(a.k)
     elif a.which == "k390-learned":
