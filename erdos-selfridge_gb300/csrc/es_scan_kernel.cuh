@@ -291,7 +291,11 @@ __device__ __forceinline__ void tail_one(const TailCtx& C, const EsFilterC* sFC,
 // its entry (the rest of the entry goes back on the queue), so the residue stage runs converged
 // and the warp leaves it as soon as no lane has a live candidate; the few candidates left take
 // n mod M and the exact tail.
-template <bool COUNT>
+// Entry formats: words (w, w + 1) of one ring-1 digit: {bits of w, bits of w + 1, d1 | split <<
+// 16, lane | wrap << 5 | w << 6}; or, with PD (one-word inner rings), the words of two
+// consecutive digits d1, d1 + 1: {bits of d1, bits of d1 + 1, d1 | split(d1) << 16 |
+// split(d1 + 1) << 24, lane | wrap(d1) << 5 | wrap(d1 + 1) << 6}.
+template <bool COUNT, bool PD>
 __device__ __forceinline__ void flush(EsQueue* Q, const unsigned char* smem, const EsInst& si, uint32_t lane,
                                       uint32_t step, uint32_t& qhead, uint32_t& qsize) {
     __syncwarp();
@@ -318,11 +322,13 @@ __device__ __forceinline__ void flush(EsQueue* Q, const unsigned char* smem, con
     qsize += __popc(back);
     const bool has = bits != 0ull;
     const uint32_t i = has ? __ffsll((long long)bits) - 1u : 0u;
-    const uint32_t d1 = has ? (en.z & 0xffffu) : 0u;
-    const uint32_t slot = has ? ((en.w >> 6) << 5) + i : 0u;
+    const uint32_t hw = PD ? (i >> 5) : 0u;        // PD: the candidate is in the second digit's word
+    const uint32_t d1 = has ? (en.z & 0xffffu) + hw : 0u;
+    const uint32_t slot = has ? (PD ? (i & 31u) : ((en.w >> 6) << 5) + i) : 0u;
     const uint32_t own = has ? (en.w & 31u) : 0u;
-    const bool wrap1 = has && ((en.w >> 5) & 1u);
-    const bool cw = has && slot >= (en.z >> 16);   // sorted slots from the split on wrap past M
+    const bool wrap1 = has && ((en.w >> (5u + hw)) & 1u);
+    const uint32_t split = PD ? (hw ? (en.z >> 24) : ((en.z >> 16) & 0xffu)) : (en.z >> 16);
+    const bool cw = has && slot >= split;          // sorted slots from the split on wrap past M
     // lanes without an entry run the residue stage's loads too: give them zero residues, not
     // another lane's record (lane 0 of a unit may not have reached its first cycle yet)
     const uint4 bq = has ? Q->rec1[own] : make_uint4(0u, 0u, 0u, 0u);
@@ -354,20 +360,27 @@ __device__ __forceinline__ void flush(EsQueue* Q, const unsigned char* smem, con
     __syncwarp();
 }
 
-// warp-uniform (has = ballot of (lo | hi) != 0, nonzero; qsize < 32 on entry): queue the word
-// pair (wd, wd + 1) of every lane that has candidates, then flush while 32 entries are waiting
-template <bool COUNT>
+// warp-uniform (has = ballot of (lo | hi) != 0, nonzero; qsize < 32 on entry): queue the entry
+// {lo, hi, ez, ew} (formats above flush) of every lane that has candidates, then flush while 32
+// entries are waiting
+template <bool COUNT, bool PD>
 __device__ __forceinline__ void push(EsQueue* Q, const unsigned char* smem, const EsInst& si, uint32_t lane,
                                      uint32_t step, uint32_t& qhead,
                                      uint32_t& qsize, uint32_t has, uint32_t lo, uint32_t hi,
-                                     uint32_t split, uint32_t d1, uint32_t wd, uint32_t wm1) {
+                                     uint32_t ez, uint32_t ew) {
     if (lo | hi) {
         const uint32_t pos = (qhead + qsize + __popc(has & ((1u << lane) - 1u))) & (ES_QCAP - 1);
-        Q->ent[pos] = make_uint4(lo, hi, d1 | (split << 16), lane | (wm1 & 32u) | (wd << 6));
+        Q->ent[pos] = make_uint4(lo, hi, ez, ew);
     }
     qsize += __popc(has);
     // each pass retires one candidate per lane, so this ends
-    while (qsize >= 32u) flush<COUNT>(Q, smem, si, lane, step, qhead, qsize);
+    while (qsize >= 32u) flush<COUNT, PD>(Q, smem, si, lane, step, qhead, qsize);
+}
+
+// entry fields of the words (wd, wd + 1) of digit d1
+__device__ __forceinline__ uint32_t ent_z(uint32_t d1, uint32_t split) { return d1 | (split << 16); }
+__device__ __forceinline__ uint32_t ent_w(uint32_t lane, uint32_t wm1, uint32_t wd) {
+    return lane | (wm1 & 32u) | (wd << 6);
 }
 
 // Warp-uniform: scan one warp-unit w of `item`, whose plan is staged in smem / si.
@@ -461,6 +474,9 @@ __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, u
     // word-mask phase tables, in global memory or staged in shared memory by the launch
     constexpr bool WMASK = LAYOUT == ES_LAYOUT_WORDMASK || LAYOUT == ES_LAYOUT_SMEM;
     constexpr bool PAIRL = LAYOUT == ES_LAYOUT_PAIR || LAYOUT == ES_LAYOUT_SMEM_PAIR;
+    // one-word inner rings on the word-by-word path queue two ring-1 digits per entry
+    constexpr bool PD = WT == 1 && !PAIRL;
+    uint32_t pbits = 0u, psplit = 0u, pwrap = 0u;   // PD: the even digit's word, waiting
     uint32_t qf[FA], corr[FA];
     const uint32_t* tab[FA];
     uint32_t tabs[FA];   // shared address of each staged table (ES_LAYOUT_SMEM, ES_LAYOUT_SMEM_PAIR)
@@ -555,6 +571,9 @@ __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, u
         const uint32_t KA = key32(sub128(Mv, b2, brA), ldv32(&si.sh));
 
         // ---- ring 1: warp-uniform sweep (broadcast loads) --------------------------------
+        // one-word rings with at most four inner filters: two digits per iteration give the
+        // scheduler independent chains (+2.4 % at k = 300); elsewhere it spills or loses
+#pragma unroll(WT == 1 && F <= 4 ? 2 : 1)
         for (uint32_t d1 = 0; d1 < r1; ++d1) {
             const bool act = (d1 - lo1) < (hi1 - lo1);          // lo1 <= d1 < hi1
             // ring-1 wrap (b2 + T1 >= M, i.e. T1 >= A) from the 32-bit keys
@@ -615,7 +634,7 @@ __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, u
                     if (COUNT) cnt[f] += __popc(b0) + __popc(b1);
                 }
                 const uint32_t has = __ballot_sync(0xffffffffu, (b0 | b1) != 0u);
-                if (has) push<COUNT>(Q, smem, si, lane, step, qhead, qsize, has, b0, b1, split, d1, 0u, wm1);
+                if (has) push<COUNT, PD>(Q, smem, si, lane, step, qhead, qsize, has, b0, b1, ent_z(d1, split), ent_w(lane, wm1, 0u));
                 continue;
             }
             if (WMASK && WT == 4) {
@@ -641,9 +660,9 @@ __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, u
                     if (COUNT) cnt[f] += __popc(b[0]) + __popc(b[1]) + __popc(b[2]) + __popc(b[3]);
                 }
                 const uint32_t h0 = __ballot_sync(0xffffffffu, (b[0] | b[1]) != 0u);
-                if (h0) push<COUNT>(Q, smem, si, lane, step, qhead, qsize, h0, b[0], b[1], split, d1, 0u, wm1);
+                if (h0) push<COUNT, PD>(Q, smem, si, lane, step, qhead, qsize, h0, b[0], b[1], ent_z(d1, split), ent_w(lane, wm1, 0u));
                 const uint32_t h1 = __ballot_sync(0xffffffffu, (b[2] | b[3]) != 0u);
-                if (h1) push<COUNT>(Q, smem, si, lane, step, qhead, qsize, h1, b[2], b[3], split, d1, 2u, wm1);
+                if (h1) push<COUNT, PD>(Q, smem, si, lane, step, qhead, qsize, h1, b[2], b[3], ent_z(d1, split), ent_w(lane, wm1, 2u));
                 continue;
             }
             if (WMASK && WT == 2) {
@@ -665,7 +684,7 @@ __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, u
                     if (COUNT) cnt[f] += __popc(b0) + __popc(b1);
                 }
                 const uint32_t has = __ballot_sync(0xffffffffu, (b0 | b1) != 0u);
-                if (has) push<COUNT>(Q, smem, si, lane, step, qhead, qsize, has, b0, b1, split, d1, 0u, wm1);
+                if (has) push<COUNT, PD>(Q, smem, si, lane, step, qhead, qsize, has, b0, b1, ent_z(d1, split), ent_w(lane, wm1, 0u));
                 continue;
             }
             uint32_t lo = 0u;   // bits of an even word, queued with the odd word after it
@@ -710,6 +729,25 @@ __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, u
                     }
                 }
                 // ---- queue the survivors of the inner-ring stage -----------------------------
+                if (PD) {
+                    // one-word ring: an even digit's word waits for the next digit's, and the two
+                    // go out as one entry (half the queue pushes)
+                    if ((d1 & 1u) == 0u && d1 + 1u < r1) {
+                        pbits = bits;
+                        psplit = split;
+                        pwrap = wm1 & 32u;
+                        continue;
+                    }
+                    const bool odd = (d1 & 1u) != 0u;
+                    const uint32_t plo = odd ? pbits : bits, phi = odd ? bits : 0u;
+                    const uint32_t has = __ballot_sync(0xffffffffu, (plo | phi) != 0u);
+                    if (has) {
+                        const uint32_t ez = odd ? ((d1 - 1u) | (psplit << 16) | (split << 24)) : ent_z(d1, split);
+                        const uint32_t ew = lane | (odd ? (pwrap | ((wm1 & 32u) << 1)) : (wm1 & 32u));
+                        push<COUNT, PD>(Q, smem, si, lane, step, qhead, qsize, has, plo, phi, ez, ew);
+                    }
+                    continue;
+                }
                 if ((wd & 1u) == 0u && wd + 1u < Wn) {
                     lo = bits;
                     continue;
@@ -717,11 +755,12 @@ __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, u
                 const bool odd = (wd & 1u) != 0u;
                 const uint32_t plo = odd ? lo : bits, phi = odd ? bits : 0u;
                 const uint32_t has = __ballot_sync(0xffffffffu, (plo | phi) != 0u);
-                if (has) push<COUNT>(Q, smem, si, lane, step, qhead, qsize, has, plo, phi, split, d1, wd & ~1u, wm1);
+                if (has) push<COUNT, PD>(Q, smem, si, lane, step, qhead, qsize, has, plo, phi, ent_z(d1, split),
+                                         ent_w(lane, wm1, wd & ~1u));
             }
         }
         // the records change with the next strip step: drain the queue
-        while (qsize) flush<COUNT>(Q, smem, si, lane, step, qhead, qsize);
+        while (qsize) flush<COUNT, PD>(Q, smem, si, lane, step, qhead, qsize);
     }
     // ---- per-stage counts of this warp-unit into the item's totals ----------------------
     if (COUNT) {

@@ -83,9 +83,12 @@ typedef struct es_tune {
     uint32_t layout;        /* ES_LAYOUT_WORDMASK, _SCALAR, _PAIR, _SMEM or _SMEM_PAIR */
     uint32_t mask_filters;  /* filters in the inner-ring stage, 1..ES_MAX_MASK_FILTERS */
     uint32_t threads;       /* CTA size, multiple of 32 in [64, 512] */
-    uint32_t strip;         /* ring-1 cycles per thread per work unit (strip depth) */
-    uint32_t smem_kb;       /* accepted, no effect: the phase tables are read through L1, which
-                               measured faster than staging them in shared memory */
+    uint32_t strip;         /* at most this many ring-1 cycles per thread per work unit: the
+                               lanes of a warp take 32 consecutive ring-2 rows over one of
+                               ceil(r2 / strip) balanced windows of ring-2 digits; lists and
+                               plans without a ring 2 take `strip` consecutive entries */
+    uint32_t smem_kb;       /* accepted, no effect (the staged layouts size their own shared
+                               memory) */
     uint32_t ctas_per_sm;   /* persistent grid = SM count * ctas_per_sm */
     uint32_t count_stages;  /* 1: accumulate per-filter-stage pass counts */
     uint32_t reserved;
