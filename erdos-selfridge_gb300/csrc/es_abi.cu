@@ -77,9 +77,9 @@ int device_facts() {
 size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 int check_tune(const es_tune& t) {
-    if (t.layout > ES_LAYOUT_SMEM_PAIR)
+    if (t.layout > ES_LAYOUT_AUTO)
         return fail(ES_ERR_ARG, "tune.layout must be 0 (word-mask), 1 (scalar), 2 (pair), 3 (word masks in shared "
-                                "memory) or 4 (pair tables in shared memory)");
+                                "memory), 4 (pair tables in shared memory) or 5 (chosen per launch)");
     if (t.mask_filters < 1 || t.mask_filters > ES_MAX_MASK_FILTERS)
         return fail(ES_ERR_ARG, "tune.mask_filters must be in 1..8");
     if (t.threads < 64 || t.threads > 1024 || t.threads % 32)
@@ -196,25 +196,41 @@ SmemPlan plan_smem(uint32_t small_max, uint32_t nf_max, const es_tune& tune, uin
     return p;
 }
 
-// Words of inner-stage tables a staged layout copies into shared memory: the word-mask tables of
-// the first F filters (ES_LAYOUT_SMEM) or their pair tables, twice the words (ES_LAYOUT_SMEM_PAIR).
-uint32_t stage_words_of(uint32_t layout, const EsInst& I, uint32_t F) {
-    if (layout == ES_LAYOUT_SMEM) return I.mask_off[F];
-    if (layout == ES_LAYOUT_SMEM_PAIR) return 2u * I.mask_off[F];
+// Words of inner-stage tables a launch of `layout` copies into shared memory, given the word-mask
+// words of its first F filters (EsInst::mask_off[F]): those words (ES_LAYOUT_SMEM), twice them as
+// pair tables (ES_LAYOUT_SMEM_PAIR), or none.
+uint32_t staged_words(uint32_t layout, uint32_t mask_words) {
+    if (layout == ES_LAYOUT_SMEM) return mask_words;
+    if (layout == ES_LAYOUT_SMEM_PAIR) return 2u * mask_words;
     return 0u;
 }
 
-// The layout a launch actually runs: a staged layout only for inner rings of one or two words
-// whose stage_words of inner-stage tables fit the opt-in shared memory beside the rest of the
-// launch's shared memory; otherwise the same tables read through L1 (word masks, or pair tables).
-// Neither choice changes which candidates pass.
+// Word-mask bytes of the inner-stage tables that fit the L1 beside the scan's own shared memory.
+constexpr uint32_t kL1TableBudget = 180u * 1024u;
+
+// The layout a launch actually runs, given the word-mask words of its inner-stage tables (the
+// largest among its plans).  A staged layout only for inner rings of one or two words whose
+// staged tables fit the opt-in shared memory beside the rest of the launch's shared memory;
+// otherwise the same tables read through L1 (word masks, or pair tables).  ES_LAYOUT_AUTO: staged
+// word masks where they fit, else word masks through L1 when those fit L1 and pair tables would
+// not, else pair tables (wider rings: word masks).  No choice changes which candidates pass.
 uint32_t launch_layout(uint32_t layout, uint32_t words, uint32_t small_max, uint32_t nf_max,
-                       const es_tune& tune, uint32_t stage_words) {
+                       const es_tune& tune, uint32_t mask_words) {
+    auto fits = [&](uint32_t l) {
+        return plan_smem(small_max, nf_max, tune, staged_words(l, mask_words)).bytes <=
+               (uint32_t)g_dev.smem_optin - 1024u;
+    };
+    const bool narrow = words == 1 || words == 2;
+    if (layout == ES_LAYOUT_AUTO) {
+        if (!narrow) return ES_LAYOUT_WORDMASK;
+        if (fits(ES_LAYOUT_SMEM)) return ES_LAYOUT_SMEM;
+        const uint64_t bytes = 4ull * mask_words;
+        return (bytes <= kL1TableBudget && kL1TableBudget < 2 * bytes) ? ES_LAYOUT_WORDMASK : ES_LAYOUT_PAIR;
+    }
     if (layout != ES_LAYOUT_SMEM && layout != ES_LAYOUT_SMEM_PAIR) return layout;
-    const uint32_t fallback = layout == ES_LAYOUT_SMEM ? ES_LAYOUT_WORDMASK : ES_LAYOUT_PAIR;
-    if (words != 1 && words != 2) return ES_LAYOUT_WORDMASK;
-    const SmemPlan p = plan_smem(small_max, nf_max, tune, stage_words);
-    return p.bytes <= (uint32_t)g_dev.smem_optin - 1024u ? layout : fallback;
+    if (!narrow) return ES_LAYOUT_WORDMASK;
+    if (fits(layout)) return layout;
+    return layout == ES_LAYOUT_SMEM ? ES_LAYOUT_WORDMASK : ES_LAYOUT_PAIR;
 }
 
 // Filters of the inner-ring stage actually compiled into the launched kernel: word-mask kernels
@@ -655,9 +671,8 @@ static int ctx_launch(es_ctx* c, uint64_t ob, uint64_t oe, const uint64_t* d_lis
     it.group = 0;
     it.inst_id = 0;
     const uint32_t F = stage_filters(tn.layout, tn.mask_filters, I.n_filters, I.F_built);
-    const uint32_t layout = launch_layout(tn.layout, I.W, I.small_bytes, I.n_filters, tn,
-                                          stage_words_of(tn.layout, I, F));
-    const SmemPlan sp = plan_smem((uint32_t)I.small_bytes, I.n_filters, tn, stage_words_of(layout, I, F));
+    const uint32_t layout = launch_layout(tn.layout, I.W, I.small_bytes, I.n_filters, tn, I.mask_off[F]);
+    const SmemPlan sp = plan_smem((uint32_t)I.small_bytes, I.n_filters, tn, staged_words(layout, I.mask_off[F]));
     it.caller = 0;
     L.items = nullptr;
     L.n_items = 1;
@@ -922,12 +937,11 @@ int es_batch_create(es_ctx* const* ctxs, uint32_t n_ctx, const es_batch_item* it
         }
         es_batch::Sub sub;
         sub.words = cls == 0 ? 0u : (cls == 4 && words == 0 ? 4u : (words ? words : cls));
-        uint32_t stage_words = 0;   // the largest inner-stage tables among the class's plans
+        uint32_t mask_words = 0;   // the largest inner-stage word-mask tables among the class's plans
         for (uint32_t j = pos; j < end; ++j)
-            stage_words = std::max<uint32_t>(stage_words,
-                                             stage_words_of(tune.layout, ctxs[items[order[j]].ctx_index]->h_inst, F));
-        sub.layout = launch_layout(tune.layout, sub.words, small_max, nf_max, tune, stage_words);
-        const SmemPlan sp = plan_smem(small_max, nf_max, tune, sub.layout == tune.layout ? stage_words : 0u);
+            mask_words = std::max<uint32_t>(mask_words, ctxs[items[order[j]].ctx_index]->h_inst.mask_off[F]);
+        sub.layout = launch_layout(tune.layout, sub.words, small_max, nf_max, tune, mask_words);
+        const SmemPlan sp = plan_smem(small_max, nf_max, tune, staged_words(sub.layout, mask_words));
         EsLaunch& L = sub.L;
         memset(&L, 0, sizeof(L));
         L.items = b->d_items_launch + pos;
@@ -1175,8 +1189,8 @@ extern "C" int es_search_blocks_static(const es_ctx* c, uint64_t t0, uint32_t n_
     const uint32_t F = stage_filters(tn.layout, tn.mask_filters, nf, I.F_built);
     es_tune tn0 = tn;
     tn0.count_stages = 0;   // the static search never counts
-    const uint32_t layout = launch_layout(tn.layout, I.W, I.small_bytes, nf, tn0, stage_words_of(tn.layout, I, F));
-    const SmemPlan sp = plan_smem((uint32_t)I.small_bytes, nf, tn0, stage_words_of(layout, I, F));
+    const uint32_t layout = launch_layout(tn.layout, I.W, I.small_bytes, nf, tn0, I.mask_off[F]);
+    const SmemPlan sp = plan_smem((uint32_t)I.small_bytes, nf, tn0, staged_words(layout, I.mask_off[F]));
     uint64_t cbeg = 0;
     const uint64_t ncyc = cycles_of(I, 0, I.n_outer, &cbeg);
     const uint64_t nu = units_of(I, cbeg, cbeg + ncyc, tn.strip);

@@ -23,7 +23,7 @@ SPACE = {
     "threads": [256, 384, 512],
     "strip": [2, 4, 8, 16],
     "mask_filters": [2, 3, 4, 5, 6],
-    "layout": [N.LAYOUT_WORDMASK, N.LAYOUT_PAIR, N.LAYOUT_SMEM, N.LAYOUT_SMEM_PAIR, N.LAYOUT_SCALAR],
+    "layout": [N.LAYOUT_WORDMASK, N.LAYOUT_PAIR, N.LAYOUT_SMEM, N.LAYOUT_SMEM_PAIR, N.LAYOUT_AUTO, N.LAYOUT_SCALAR],
 }
 DEFAULT = dict(layout=N.LAYOUT_WORDMASK, mask_filters=4, threads=512, strip=8, smem_kb=0,
                ctas_per_sm=4, count_stages=0)

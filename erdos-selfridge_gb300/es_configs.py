@@ -64,10 +64,12 @@ def small_k(ks=range(40, 121), known: dict | None = None) -> dict:
             "all_match": all(v["match"] for v in out.values()) if known else None}
 
 
-def batch64(seed: int = 0, autotune: bool = True, reps: int = 5, items_log2: int = 24) -> dict:
+def batch64(seed: int = 0, autotune: bool = True, reps: int = 5, items_log2: int = 24,
+            tune: dict | None = None) -> dict:
     """Config 3.  Besides the timings it returns, for every instance of at most 2^items_log2
     positions, the survivors and per-stage counts of a counting batch (``small_items``), which
-    the GPU tests check against the oracle."""
+    the GPU tests check against the oracle.  The launch shape starts from the library's per-class
+    layout choice (ES_LAYOUT_AUTO) and `tune`; the autotuner then searches from there."""
     ks, L = batch64_instances(seed)
     plans = [es_gb300.Plan(k) for k in ks]
     tune0 = N.make_tune(**es_autotune.DEFAULT)
@@ -77,8 +79,9 @@ def batch64(seed: int = 0, autotune: bool = True, reps: int = 5, items_log2: int
         n_outer = -(-min(length, p.R) // c.r0)
         items.append((i, i, 0, 0, n_outer))
         positions += n_outer * c.r0
-    tune, tune_ms = (es_autotune.tune_batch(ctxs, items) if autotune
-                     else (dict(es_autotune.DEFAULT), None))
+    start = dict(es_autotune.DEFAULT, layout=N.LAYOUT_AUTO)
+    start.update(tune or {})
+    tune, tune_ms = (es_autotune.tune_batch(ctxs, items, start=start) if autotune else (start, None))
     b = N.Batch(ctxs, items, N.make_tune(**tune))
     b.run(use_graph=True)
     b.sync()
@@ -269,13 +272,13 @@ def main():
     ap.add_argument("--log2-positions", type=int, default=40)
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--tune", type=json.loads, default=None,
-                    help="k390: launch shape (JSON, es_autotune.DEFAULT keys) instead of the default")
+                    help="k390, batch64: launch shape (JSON, es_autotune.DEFAULT keys) instead of the default")
     a = ap.parse_args()
     if a.which == "small-k":
         known = {k: g for k, (g, _) in es_gb300.load_known(a.bfile).items()} if a.bfile else None
         out = small_k(known=known)
     elif a.which == "batch64":
-        out = batch64(autotune=not a.no_autotune)
+        out = batch64(autotune=not a.no_autotune, tune=a.tune)
     elif a.which == "k390":
         orders = None
         if a.model:   # the learned planner's cascade order for each wheel

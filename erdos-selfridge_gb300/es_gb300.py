@@ -202,7 +202,8 @@ class GpuSieve:
         self.launches = 0
         self.residues_checked = 0
         self.mask_mode = {N.LAYOUT_SCALAR: "scalar-gb300", N.LAYOUT_PAIR: "pair-gb300",
-                          N.LAYOUT_SMEM: "smem-gb300", N.LAYOUT_SMEM_PAIR: "smem-pair-gb300"}.get(
+                          N.LAYOUT_SMEM: "smem-gb300", N.LAYOUT_SMEM_PAIR: "smem-pair-gb300",
+                          N.LAYOUT_AUTO: "auto-gb300"}.get(
             self.tune.layout, "wordmask-gb300")
         self.tconst = _Tconst(self)
         self.out_n = _OutN(self)

@@ -22,6 +22,7 @@ LAYOUT_SCALAR = 1
 LAYOUT_PAIR = 2       # word masks with the wrapped row beside each phase (inner rings <= 64 slots)
 LAYOUT_SMEM = 3       # word masks of the inner-stage filters staged in shared memory (<= 64 slots)
 LAYOUT_SMEM_PAIR = 4  # pair tables of the inner-stage filters staged in shared memory (<= 64 slots)
+LAYOUT_AUTO = 5       # chosen per launch (per width class in a batch) by the library
 MAX_MASK_FILTERS = 8
 
 

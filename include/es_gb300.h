@@ -49,6 +49,10 @@ extern "C" {
 #define ES_LAYOUT_SMEM_PAIR 4 /* the pair tables of the inner-stage filters copied into shared
                                  memory the same way (one 8- or 16-byte load per filter and word;
                                  otherwise the launch uses ES_LAYOUT_PAIR) */
+#define ES_LAYOUT_AUTO 5      /* chosen per launch from the inner-stage tables' bytes: staged word
+                                 masks where they fit, else word masks through L1 when they fit
+                                 L1 and pair tables would not, else pair tables (rings of three
+                                 or more words: word masks); a batch decides per width class */
 
 #define ES_MAX_MASK_FILTERS 8 /* filters evaluated in the inner-ring stage */
 #define ES_MAX_Q (1u << 20)   /* filter moduli q = p^t_p must be below 2^20 (k <= 1024) */
@@ -80,7 +84,7 @@ typedef struct es_plan_desc {
 /* Launch shape and table layout; chosen by the autotuner (es_autotune.py).  None of these
  * changes which candidates pass. */
 typedef struct es_tune {
-    uint32_t layout;        /* ES_LAYOUT_WORDMASK, _SCALAR, _PAIR, _SMEM or _SMEM_PAIR */
+    uint32_t layout;        /* ES_LAYOUT_WORDMASK, _SCALAR, _PAIR, _SMEM, _SMEM_PAIR or _AUTO */
     uint32_t mask_filters;  /* filters in the inner-ring stage, 1..ES_MAX_MASK_FILTERS */
     uint32_t threads;       /* CTA size, multiple of 32 in [64, 512] */
     uint32_t strip;         /* at most this many ring-1 cycles per thread per work unit: the

@@ -28,6 +28,7 @@ SHAPES = [
     dict(layout=4, mask_filters=5, threads=256, strip=3),
     dict(layout=3, mask_filters=4, threads=512, strip=8),
     dict(layout=0, mask_filters=3, threads=256, strip=64),   # windows wider than ring 2
+    dict(layout=5, mask_filters=4, threads=512, strip=8),    # chosen per launch
 ]
 
 
@@ -204,9 +205,10 @@ def test_batch64_prefixes(native):
         ctxs.append(N.Context(plan, _tune(N)))
         items.append((i, i, 0, 0, inst["prefix_outer"]))
     # the plans differ in inner-ring width: one launch per width class; with layout 2 the one-
-    # and two-word classes use pair tables and the three-word class the 16-byte-row word masks
-    for graph, layout in ((False, 0), (True, 0), (False, 2)):
-        b = N.Batch(ctxs, items, _tune(N, layout=layout, mask_filters=6, strip=2))
+    # and two-word classes use pair tables and the three-word class the 16-byte-row word masks;
+    # layout 5 lets the library choose per class (staged word masks where they fit at F = 4)
+    for graph, layout, F in ((False, 0, 6), (True, 0, 6), (False, 2, 6), (True, 5, 6), (False, 5, 4)):
+        b = N.Batch(ctxs, items, _tune(N, layout=layout, mask_filters=F, strip=2))
         b.run(use_graph=graph)
         b.sync()
         surv = b.survivors()

@@ -146,7 +146,7 @@ def test_run_k_masks_found_pause_resume_and_mask_mode(driver, monkeypatch, tmp_p
                                           "--max-launches", "3"])
     assert r1["status"] == "PAUSED" and 0 < r1["unit_done"] < r1["units_total"]
     state = json.load(open(tmp_path / f"k{k}_paused.json"))
-    assert state["mask_mode"] in ("wordmask-gb300", "pair-gb300", "smem-gb300", "smem-pair-gb300",
+    assert state["mask_mode"] in ("wordmask-gb300", "pair-gb300", "smem-gb300", "smem-pair-gb300", "auto-gb300",
                                   "scalar-gb300")
     r2 = _cli(masks, monkeypatch, base + ["--tag", "paused", "--ckpt-every", "1e9"])
     assert r2["status"] == "FOUND" and r2["g"] == res["g"] and r2["restarts"] == 1
