@@ -205,6 +205,9 @@ uint32_t staged_words(uint32_t layout, uint32_t mask_words) {
     return 0u;
 }
 
+// Launches per batch: four width classes, each split into staged and unstaged plans.
+constexpr uint32_t kMaxSubs = 8;
+
 // Word-mask bytes of the inner-stage tables that fit the L1 beside the scan's own shared memory.
 constexpr uint32_t kL1TableBudget = 180u * 1024u;
 
@@ -881,13 +884,25 @@ int es_batch_create(es_ctx* const* ctxs, uint32_t n_ctx, const es_batch_item* it
     }
     b->n_groups = max_group + 1;
     b->counts_words = cwords;
-    // launch order: items grouped by width class (stable), one launch per class
+    // launch order: items grouped by width class (stable), one launch per class; with
+    // ES_LAYOUT_AUTO a one- or two-word class splits further into the plans whose inner-stage
+    // tables fit shared memory (staged) and the rest
+    auto class_key = [&](uint32_t item) -> uint32_t {
+        const EsInst& I = ctxs[items[item].ctx_index]->h_inst;
+        uint32_t key = 2u * width_class(I.W);
+        if (tune.layout == ES_LAYOUT_AUTO && (I.W == 1 || I.W == 2)) {
+            const uint32_t Fi = stage_filters(tune.layout, tune.mask_filters, I.n_filters, I.F_built);
+            if (launch_layout(ES_LAYOUT_AUTO, I.W, (uint32_t)I.small_bytes, I.n_filters, tune, I.mask_off[Fi]) ==
+                ES_LAYOUT_SMEM)
+                key += 1u;
+        }
+        return key;
+    };
+    std::vector<uint32_t> keys(n_items);
+    for (uint32_t i = 0; i < n_items; ++i) keys[i] = class_key(i);
     std::vector<uint32_t> order(n_items);
     for (uint32_t i = 0; i < n_items; ++i) order[i] = i;
-    std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) {
-        return width_class(ctxs[items[x].ctx_index]->h_inst.W) < width_class(ctxs[items[y].ctx_index]->h_inst.W);
-    });
-    const uint32_t kMaxSubs = 4;
+    std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) { return keys[x] < keys[y]; });
     cudaError_t ce = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
     if (ce == cudaSuccess) ce = cudaEventCreate(&b->ev0);
     if (ce == cudaSuccess) ce = cudaEventCreate(&b->ev1);
@@ -921,7 +936,7 @@ int es_batch_create(es_ctx* const* ctxs, uint32_t n_ctx, const es_batch_item* it
         bool one_ctx = true;
         uint32_t words = ctxs[first_ctx]->h_inst.W;
         uint64_t units = 0;
-        while (end < n_items && width_class(ctxs[items[order[end]].ctx_index]->h_inst.W) == cls) {
+        while (end < n_items && keys[order[end]] == keys[order[pos]]) {
             const uint32_t ci = items[order[end]].ctx_index;
             const es_ctx* c = ctxs[ci];
             small_max = std::max<uint32_t>(small_max, c->h_inst.small_bytes);
@@ -981,7 +996,7 @@ int es_batch_create(es_ctx* const* ctxs, uint32_t n_ctx, const es_batch_item* it
 }
 
 static int batch_enqueue(es_batch* b) {
-    ES_CUDA(cudaMemsetAsync(b->d_surv_n, 0, 8ull * 5, b->stream), "memset");   // count + unit counters
+    ES_CUDA(cudaMemsetAsync(b->d_surv_n, 0, 8ull * (1 + kMaxSubs), b->stream), "memset");   // count + unit counters
     ES_CUDA(cudaMemsetAsync(b->d_found, 0xff, 8ull * b->n_groups, b->stream), "memset");
     ES_CUDA(cudaMemsetAsync(b->d_item_next, 0, 8ull * b->n_items, b->stream), "memset");
     if (b->counts_words)
