@@ -143,3 +143,41 @@ class KernelModel:
                     if ok:
                         surv.append(int(oidx) * r0 + self.I0[slot])
         return sorted(surv), counts
+
+
+def units_of(c_begin: int, c_end: int, r2: int, strip: int) -> int:
+    """Warp-units of the ring-1 cycles [c_begin, c_end) (csrc/es_abi.cu units_of)."""
+    if c_end <= c_begin:
+        return 0
+    if r2 <= 1:
+        return -(-(c_end - c_begin) // (32 * strip))
+    rows = -(-c_end // r2) - c_begin // r2
+    return -(-rows // 32) * -(-r2 // strip)
+
+
+def unit_cycles(u: int, lane: int, c_begin: int, c_end: int, r2: int, strip: int) -> list[int]:
+    """The cycles lane `lane` of warp-unit `u` scans, in step order (scan_unit in
+    csrc/es_scan_kernel.cuh): with a ring 2, rows row0 + 32 (u // J) + lane over the balanced
+    digit window j = u mod J of J = ceil(r2 / strip); without one, `strip` consecutive cycles
+    per lane."""
+    if r2 > 1:
+        J = -(-r2 // strip)
+        rb, j = divmod(u, J)
+        wlo, whi = j * r2 // J, (j + 1) * r2 // J
+        e_lo = (c_begin // r2 + 32 * rb) * r2 + wlo + lane * r2
+        return [e for e in range(e_lo, e_lo + (whi - wlo)) if c_begin <= e < c_end]
+    e_lo = c_begin + (32 * u + lane) * strip
+    return [e for e in range(e_lo, e_lo + strip) if e < c_end]
+
+
+def pair_entry(d1: int, split_lo: int, wrap_lo: bool, split_hi: int, wrap_hi: bool, lane: int) -> tuple[int, int]:
+    """Fields z, w of a queue entry holding the words of ring-1 digits d1 (even) and d1 + 1 of a
+    one-word inner ring (push in csrc/es_scan_kernel.cuh)."""
+    return d1 | split_lo << 16 | split_hi << 24, lane | int(wrap_lo) << 5 | int(wrap_hi) << 6
+
+
+def pair_candidate(z: int, w: int, i: int) -> tuple[int, int, int, bool, int]:
+    """(d1, slot, split, wrap, lane) of candidate bit i in [0, 64) of a paired entry (flush)."""
+    hw = i >> 5
+    split = (z >> 24) if hw else (z >> 16) & 0xFF
+    return (z & 0xFFFF) + hw, i & 31, split, bool((w >> (5 + hw)) & 1), w & 31

@@ -64,3 +64,46 @@ def test_incremental_identity():
                     assert m % q == n % q
                     total += 1
     assert total > 1000
+
+
+def test_unit_mapping_covers_every_cycle_once():
+    """The warp-unit decode (lanes on consecutive ring-2 rows, balanced digit windows) covers
+    every ring-1 cycle of a range exactly once, for ranges that start and end inside a ring-2
+    row, strips narrower and wider than ring 2, and plans without a ring 2; all lanes of a warp
+    share the ring-2 digit at every step."""
+    from kernel_model import unit_cycles, units_of
+    rng = np.random.default_rng(5)
+    for r2 in (1, 2, 13, 21, 32):
+        for strip in (1, 2, 3, 4, 7, 8, 16, 64):
+            for _ in range(6):
+                cb = int(rng.integers(0, 5000))
+                ce = cb + int(rng.integers(0, 3000))
+                seen = []
+                for u in range(units_of(cb, ce, r2, strip)):
+                    lanes = [unit_cycles(u, lane, cb, ce, r2, strip) for lane in range(32)]
+                    seen += [e for cyc in lanes for e in cyc]
+                    if r2 > 1:   # every lane's digits lie in the unit's one window
+                        J = -(-r2 // strip)
+                        bounds = [(j * r2 // J, (j + 1) * r2 // J) for j in range(J)]
+                        digits = {e % r2 for cyc in lanes for e in cyc}
+                        windows = {j for j, (lo, hi) in enumerate(bounds) for d in digits if lo <= d < hi}
+                        assert len(windows) <= 1, (r2, strip, u)
+                        assert max(hi - lo for lo, hi in bounds) <= strip
+                assert sorted(seen) == list(range(cb, ce)), (r2, strip, cb, ce)
+
+
+def test_paired_digit_entries_round_trip():
+    """A one-word ring's entry for digits d1, d1 + 1 gives back each candidate's digit, slot,
+    carry split and ring-1 wrap."""
+    from kernel_model import pair_candidate, pair_entry
+    rng = np.random.default_rng(9)
+    for _ in range(2000):
+        d1 = 2 * int(rng.integers(0, 30000))
+        sl, sh = int(rng.integers(0, 33)), int(rng.integers(0, 33))
+        wl, wh = bool(rng.integers(0, 2)), bool(rng.integers(0, 2))
+        lane = int(rng.integers(0, 32))
+        z, w = pair_entry(d1, sl, wl, sh, wh, lane)
+        for i in (0, 31, 32, 63, int(rng.integers(0, 64))):
+            got = pair_candidate(z, w, i)
+            want = (d1 + (i >> 5), i & 31, sh if i >= 32 else sl, wh if i >= 32 else wl, lane)
+            assert got == want
