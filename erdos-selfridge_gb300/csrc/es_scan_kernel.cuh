@@ -15,8 +15,8 @@
 //    single-plan launch, one per item when a launch holds several plans) -- no spin waits
 //    anywhere.  A group's later blocks are skipped once a good survivor is known (block-ordered
 //    search).
-//  * Two-level strip mining.  A lane owns `strip` consecutive ring-1 cycles (cycle index =
-//    oidx / r1).  Rings >= 2 give b2 = sum term_j mod M, decoded once per strip and then
+//  * Two-level strip mining.  A lane owns up to `strip` consecutive ring-1 cycles (cycle index
+//    = oidx / r1).  Rings >= 2 give b2 = sum term_j mod M, decoded once per strip and then
 //    stepped with a 128-bit delta table when the ring-2 digit advances.  The 32 lanes of a warp
 //    take 32 consecutive ring-2 rows over the same window of ring-2 digits, so the per-step
 //    delta rows are broadcast loads (lanes on different digits of a 21-digit ring 2 read up to

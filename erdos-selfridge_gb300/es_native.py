@@ -196,7 +196,9 @@ def layout_for(r0: int, filter_q, mask_filters: int) -> int:
     4- or 8-byte gather from shared memory costs a few bank wavefronts instead of one L1 sector
     per lane: 1.17x at k = 300).  Otherwise pair tables cost one load per filter and word instead
     of two, but twice the bytes: they win unless the word-mask tables fit L1 and the pair tables
-    do not (k = 390 gains about 1.3x from pairs).  Neither choice changes which candidates pass."""
+    do not (k = 390 gains about 1.3x from pairs).  Neither choice changes which candidates pass.
+    The library applies the same rule per launch to LAYOUT_AUTO (launch_layout in
+    csrc/es_abi.cu), with the exact shared-memory figure of the launch."""
     W = -(-max(1, int(r0)) // 32)
     if W > 2:
         return LAYOUT_WORDMASK
