@@ -383,6 +383,33 @@ __device__ __forceinline__ uint32_t ent_w(uint32_t lane, uint32_t wm1, uint32_t 
     return lane | (wm1 & 32u) | (wd << 6);
 }
 
+// The exact carry split of digit d1 for a lane whose key difference sits in the +-1 band (or ties
+// with A): b = b2 + T1[d1] in 128 bits, thr = M - b, then the first sorted slot whose term is
+// >= thr, found from the bucket of thr's key (S0[r0] = M stops the walk).  Also returns the
+// exact ring-1 wrap in wm1.  It runs for a tiny share of (lane, digit) pairs; one-word rings
+// call it out of line (rare_split_call), which frees registers in their sweep (+1.9 % at
+// k = 300), while wider rings keep it inline (out of line they lose 1-3 %).
+__device__ __forceinline__ uint32_t rare_split(EsQueue* Q, const unsigned char* smem, const EsInst& si, uint32_t lane,
+                                               uint32_t d1, uint32_t bsh, uint32_t& wm1) {
+    uint32_t wx, brw;
+    const U4 Mr = ldv_M(si);
+    const U4 b = addmod(ldv128(&Q->rec0[lane]), ldv128(smem + ldv32(&si.o_T1) + 16u * d1), Mr, wx);
+    wm1 = wx;
+    const U4 thr = sub128(Mr, b, brw);
+    const uint32_t te = key32(thr, ldv32(&si.sh));
+    const uint32_t* rK0 = reinterpret_cast<const uint32_t*>(smem + ldv32(&si.o_K0));
+    const uint4* rS0 = reinterpret_cast<const uint4*>(smem + ldv32(&si.o_S0));
+    const uint4* sBK = reinterpret_cast<const uint4*>(smem + si.o_BK);
+    uint32_t split = sBK[te >> bsh].x;
+    while (rK0[split] < te) ++split;
+    while (rK0[split] == te && lt128(u4(rS0[split]), thr)) ++split;
+    return split;
+}
+__device__ __noinline__ uint32_t rare_split_call(EsQueue* Q, const unsigned char* smem, const EsInst& si,
+                                                 uint32_t lane, uint32_t d1, uint32_t bsh, uint32_t& wm1) {
+    return rare_split(Q, smem, si, lane, d1, bsh, wm1);
+}
+
 // Warp-uniform: scan one warp-unit w of `item`, whose plan is staged in smem / si.
 template <int F, int LAYOUT, bool COUNT, int WT>
 __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, unsigned char* smem,
@@ -597,19 +624,9 @@ __device__ __forceinline__ void scan_unit(const EsLaunch& L, const EsInst& si, u
             // (only lanes with candidates here: their record holds b2)
             const bool rare = act && ((k1 == KA) || (ks <= th));
             if (__any_sync(0xffffffffu, rare)) {
-                if (rare) {
-                    uint32_t wx, brw;
-                    const U4 Mr = ldv_M(si);
-                    const U4 b = addmod(ldv128(&Q->rec0[lane]), ldv128(smem + ldv32(&si.o_T1) + 16u * d1), Mr, wx);
-                    wm1 = wx;
-                    const U4 thr = sub128(Mr, b, brw);
-                    const uint32_t te = key32(thr, ldv32(&si.sh));
-                    const uint32_t* rK0 = reinterpret_cast<const uint32_t*>(smem + ldv32(&si.o_K0));
-                    const uint4* rS0 = reinterpret_cast<const uint4*>(smem + ldv32(&si.o_S0));
-                    split = sBK[te >> bsh].x;
-                    while (rK0[split] < te) ++split;
-                    while (rK0[split] == te && lt128(u4(rS0[split]), thr)) ++split;   // S0[r0] = M stops it
-                }
+                if (rare)
+                    split = WT == 1 ? rare_split_call(Q, smem, si, lane, d1, bsh, wm1)
+                                    : rare_split(Q, smem, si, lane, d1, bsh, wm1);
             }
 
             if (PAIRL) {
