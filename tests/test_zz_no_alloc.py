@@ -39,12 +39,13 @@ def _key(recs, t_max):
 
 @pytest.mark.parametrize("k,t0,nb,count_stages,layout", [(60, 0, 16, 0, 0), (97, 0, 8, 0, 0), (70, 3, 20, 0, 0),
                                                          (30, 0, 12, 0, 0), (57, 0, 10, 1, 0), (97, 0, 8, 0, 3),
-                                                         (97, 0, 8, 0, 4)])
+                                                         (97, 0, 8, 0, 4), (300, 0, 2, 0, 5)])
 def test_static_search_matches_batch(native, bfile, k, t0, nb, count_stages, layout):
     """Two calls in a row against the allocating batch path, and the least n against g(k) of the
     b-file (every block before g(k)'s holds no good survivor).  A context built for counting
     launches works too (the static search never counts), and so does one whose launches stage
-    the phase tables in shared memory (word masks, layout 3, or pair tables, layout 4)."""
+    the phase tables in shared memory (word masks, layout 3, or pair tables, layout 4), and one whose
+    layout the library picks per launch (layout 5; at k = 300 the staged word masks)."""
     import torch
     import es_gb300
     N = native
