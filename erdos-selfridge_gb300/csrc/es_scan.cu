@@ -6,6 +6,10 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <map>
+#include <mutex>
+#include <tuple>
+
 #include "../../include/es_gb300.h"
 #include "es_internal.h"
 
@@ -157,11 +161,31 @@ int es_scan_prepare(int smem_optin_bytes) {
     return 0;
 }
 
+// Resident CTAs per SM of one instance and launch shape, cached: every launch asks, and the
+// answer only depends on the instance, the CTA size and the shared memory.
 int es_scan_occupancy(int layout, int count, uint32_t words, uint32_t mask_filters, int threads,
                       int smem_bytes, int* ctas_per_sm) {
     const ScanFn fn = pick(layout, count, words, mask_filters);
     if (!fn) return (int)cudaErrorInvalidDeviceFunction;
-    return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm, fn, threads, (size_t)smem_bytes);
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const auto key = std::make_tuple(reinterpret_cast<const void*>(fn), threads, smem_bytes, dev);
+    static std::mutex mu;
+    static std::map<std::tuple<const void*, int, int, int>, int> cache;
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        const auto it = cache.find(key);
+        if (it != cache.end()) {
+            *ctas_per_sm = it->second;
+            return 0;
+        }
+    }
+    const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm, fn, threads, (size_t)smem_bytes);
+    if (e == cudaSuccess) {
+        std::lock_guard<std::mutex> lock(mu);
+        cache[key] = *ctas_per_sm;
+    }
+    return (int)e;
 }
 
 int es_launch_scan(const EsLaunch& L, int layout, int count, uint32_t words, int grid, void* stream) {

@@ -161,6 +161,9 @@ class _OutSlice:
         self._s, self._sl = sieve, sl
 
     def get(self) -> np.ndarray:
+        stop = self._sl.stop
+        if stop is not None and self._sl.start in (None, 0) and self._sl.step in (None, 1) and stop >= 0:
+            return self._s.ctx.survivors(int(stop))   # out[:n] with n from out_n.get()
         return self._s.ctx.survivors()[self._sl]
 
 

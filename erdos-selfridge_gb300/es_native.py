@@ -309,7 +309,15 @@ class Context:
         check(lib().es_survivor_count(self.h, C.byref(n)))
         return n.value
 
-    def survivors(self) -> np.ndarray:
+    def survivors(self, n: int | None = None) -> np.ndarray:
+        """Survivor position indices.  With `n` (a count the caller already read) the first n of
+        them, read without counting twice when there are no more than n."""
+        if n is not None:
+            out = np.zeros(max(n, 1), dtype=np.uint64)
+            got = C.c_uint64()
+            if lib().es_read_survivors(self.h, _ptr(out, C.c_uint64), out.size, C.byref(got)) == 0:
+                return out[:min(got.value, n)]
+            return self.survivors()[:n]   # more than n, or an overflow (raised there)
         n = self.count()
         out = np.zeros(max(n, 1), dtype=np.uint64)
         got = C.c_uint64()

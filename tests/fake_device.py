@@ -36,10 +36,11 @@ class FakeCtx:
     def count(self):
         return len(self.surv)
 
-    def survivors(self):
+    def survivors(self, n=None):
         if len(self.surv) > self.capacity:
             raise RuntimeError("overflow")
-        return np.array(self.surv, dtype=np.uint64)
+        out = np.array(self.surv, dtype=np.uint64)
+        return out if n is None else out[:n]
 
 
 class FakeBatch:
