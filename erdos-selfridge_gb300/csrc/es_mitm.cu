@@ -21,9 +21,11 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <new>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/es_gb300.h"
@@ -210,6 +212,54 @@ int es_mitm_destroy(es_mitm* m) {
     return ES_OK;
 }
 
+namespace {
+
+// Sorts v (values below 2^bits) on the host cores: each thread counts its share of the values
+// per partition of their top P bits, the values are scattered to their partitions, and the
+// partitions are sorted, shared out among the threads.  The result equals std::sort's.
+void parallel_sort(std::vector<u128m>& v, uint32_t bits) {
+    const size_t n = v.size();
+    const unsigned T = std::max(1u, std::min(64u, std::thread::hardware_concurrency()));
+    if (n < (1u << 16) || T == 1 || bits == 0) {
+        std::sort(v.begin(), v.end());
+        return;
+    }
+    const uint32_t P = std::min<uint32_t>(12, bits);
+    const uint32_t sh = bits - P;
+    const size_t np = (size_t)1 << P;
+    auto run = [T](auto&& body) {
+        std::vector<std::thread> th;
+        for (unsigned t = 0; t < T; ++t) th.emplace_back(body, t);
+        for (auto& x : th) x.join();
+    };
+    std::vector<std::vector<size_t>> at(T, std::vector<size_t>(np, 0));
+    run([&](unsigned t) {
+        for (size_t i = n * t / T, e = n * (t + 1) / T; i < e; ++i) ++at[t][(size_t)(v[i] >> sh)];
+    });
+    std::vector<size_t> start(np + 1);
+    size_t acc = 0;
+    for (size_t p = 0; p < np; ++p) {   // partition-major, thread-minor write positions
+        start[p] = acc;
+        for (unsigned t = 0; t < T; ++t) {
+            const size_t c = at[t][p];
+            at[t][p] = acc;
+            acc += c;
+        }
+    }
+    start[np] = acc;
+    std::vector<u128m> out(n);
+    run([&](unsigned t) {
+        for (size_t i = n * t / T, e = n * (t + 1) / T; i < e; ++i) out[at[t][(size_t)(v[i] >> sh)]++] = v[i];
+    });
+    std::atomic<size_t> next(0);
+    run([&](unsigned) {
+        for (size_t p = next++; p < np; p = next++) std::sort(out.begin() + start[p], out.begin() + start[p + 1]);
+    });
+    v.swap(out);
+}
+
+}  // namespace
+
 int es_mitm_create(const es_mitm_desc* d, es_mitm** out) {
     if (!d || !out) return mfail(ES_ERR_ARG, "null descriptor or output pointer");
     *out = nullptr;
@@ -275,10 +325,10 @@ int es_mitm_create(const es_mitm_desc* d, es_mitm** out) {
         S2.swap(next);
         pos += r2[j];
     }
-    std::sort(S2.begin(), S2.end());
-    // directory over the top bits of values < M: about four entries per bucket
-    uint32_t bits = 0;
+    uint32_t bits = 0;   // values < M < 2^bits
     for (u128m x = M - 1; x; x >>= 1) ++bits;
+    parallel_sort(S2, bits);
+    // directory over the top bits of values < M: about four entries per bucket
     uint32_t D = 8;
     while (D < 26 && (1ull << (D + 2)) < n2) ++D;
     if (D > bits) D = bits;
