@@ -379,7 +379,7 @@ def test_autotune_plan_shape_is_exact(native, tmp_path):
     cache = str(tmp_path / "tune.json")
     space = {"strip": [1, 2, 4], "mask_filters": [3, 4, 5], "layout": [0, 2, 1], "threads": [256, 512]}
     tune = es_autotune.tune_plan(plan, probe_log2=26, cache=cache, space=space)
-    assert all(tune[key] in vals for key, vals in es_autotune.SPACE.items()), tune
+    assert all(tune[key] in vals for key, vals in space.items()), tune
     assert es_autotune.tune_plan(plan, probe_log2=26, cache=cache, space=space) == tune
     ctx = N.Context(plan, N.make_tune(**dict(tune, count_stages=1)))
     ob = 31337
