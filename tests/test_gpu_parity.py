@@ -368,9 +368,10 @@ def test_k390_autotuned_config_vs_c_oracle(native):
 
 
 def test_autotune_plan_shape_is_exact(native, tmp_path):
-    """es_autotune.tune_plan on a small plan: the shape it returns lies in its search space, is
-    cached (a second call returns it without timing), and the survivors and per-stage counts under
-    it equal the C oracle's."""
+    """es_autotune.tune_plan on a small plan: every field of the shape it returns is the start
+    shape's (the default with the layout rule's layout) or a value of the search space, the shape
+    is cached (a second call returns it without timing), and the survivors and per-stage counts
+    under it equal the C oracle's."""
     import es_autotune
     import es_gb300
     import es_oracle as O
@@ -379,7 +380,8 @@ def test_autotune_plan_shape_is_exact(native, tmp_path):
     cache = str(tmp_path / "tune.json")
     space = {"strip": [1, 2, 4], "mask_filters": [3, 4, 5], "layout": [0, 2, 1], "threads": [256, 512]}
     tune = es_autotune.tune_plan(plan, probe_log2=26, cache=cache, space=space)
-    assert all(tune[key] in vals for key, vals in space.items()), tune
+    start = dict(es_autotune.DEFAULT, layout=N.layout_for_plan(plan, es_autotune.DEFAULT["mask_filters"]))
+    assert all(tune[key] in vals or tune[key] == start[key] for key, vals in space.items()), tune
     assert es_autotune.tune_plan(plan, probe_log2=26, cache=cache, space=space) == tune
     ctx = N.Context(plan, N.make_tune(**dict(tune, count_stages=1)))
     ob = 31337
