@@ -13,9 +13,12 @@ Prints one JSON line (rank 0).  ``value`` is device-timed (CUDA events on the en
 L2 flushed by a 256 MiB write between timed steps) on the production path (stage counting
 off); one untimed counting pass over the same range supplies the per-stage pass counts.
 ``e2e`` is the same metric through the drop-in GpuSieve API with host buffers (block constants
-in; survivor count and survivors out).  ``roofline`` uses the integer-op model W(k) = 10 + 8 f(k) int32 ops per candidate
-(f = mean filter evaluations per candidate, from this run's own stage counts) against the
-measured int32 peak of the integer-pipe microbenchmark in the same run.
+in; survivor count and survivors out).  ``roofline.frac`` is the measured integer-op rate (ncu
+integer thread-instructions per candidate, stored with the launch shape they were captured on,
+times this run's Gcand/s) against the integer peak the LOP3 + IMAD microbenchmark measures in
+the same run; ``roofline.issue`` is the same for warp instructions against the issue peak; and
+``roofline.model_frac`` is the reference's scalar model W(k) = 10 + 8 f(k) int32 ops per candidate
+(f = mean filter evaluations per candidate, from this run's own stage counts) against that peak.
 """
 from __future__ import annotations
 
